@@ -1,0 +1,20 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _oracle_built():
+    """Builds the CPU oracle (and, where the reference sources exist, the reference library)."""
+    from oracle import oracle as O
+    O.build()
+    yield

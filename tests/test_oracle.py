@@ -1,0 +1,159 @@
+"""The CPU oracle pinned against the reference: golden vectors (always) and the reference library
+itself (where it was built from the reference sources). CPU only."""
+import numpy as np
+import pytest
+
+from golden_io import Golden, by_id, names, rel_rms
+from lettuce_simulate_physics_gb300 import scenarios as S
+from oracle import oracle as O
+
+TREE_FIXTURES = names("tree_")
+FORCE_FIXTURES = names("direct_") + names("tree_") + names("small_")
+
+
+def _zero_v(b):
+    b = b.copy()
+    b.vx[:] = 0
+    b.vy[:] = 0
+    b.vz[:] = 0
+    return b
+
+
+def _run(kind, b, method, G, eps, theta, pot):
+    be = O.OracleBackend(kind, 0)
+    be.upload(_zero_v(b))
+    be.compute_forces(method, G, eps, theta, pot)
+    return be
+
+
+THETA = {"t06": 0.6, "t03": 0.3, "t00": 0.0}
+
+
+@pytest.mark.parametrize("name", TREE_FIXTURES)
+def test_port_tree_bit_exact_vs_reference_golden(name):
+    g = Golden(name)
+    b = g.inputs()
+    for c in g.cases():
+        ref = g.case(c)
+        be = _run("port", b, O.TREE, g.param("G"), g.param("eps"), THETA[c], bool(ref["has_pe"]))
+        assert np.array_equal(be.keys(), ref["keys"]), "Morton keys"
+        assert np.array_equal(be.download().id, ref["order_id"]), "sort permutation"
+        nodes = be.nodes()
+        assert len(nodes) == len(ref["nodes"])
+        for f in ("first", "nchild", "lo", "hi"):
+            assert np.array_equal(nodes[f], ref["nodes"][f]), f
+        for f in ("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz"):
+            assert np.array_equal(nodes[f], ref["nodes"][f]), f
+        np.testing.assert_allclose(nodes["rcrit2"], ref["nodes"]["rcrit2"], rtol=2e-7, atol=0)
+        assert np.array_equal(be.geo(), ref["geo"])
+        assert np.array_equal(be.groups(), ref["groups"])
+        assert np.array_equal(be.leaves(), ref["leaves"])
+        assert be.max_depth() == int(ref["max_depth"])
+        t = be.times()
+        assert t["interactions"] == int(ref["interactions"])
+        assert np.array_equal(be.body_costs(), ref["costs"])
+        e = rel_rms(be.accel()[:3], ref["acc"][:3])
+        assert e <= 1e-6, e
+
+
+@pytest.mark.parametrize("name", names("direct_") + names("small_"))
+def test_port_direct_vs_reference_golden(name):
+    g = Golden(name)
+    b = g.inputs()
+    for c in g.cases():
+        ref = g.case(c)
+        method = O.TREE if c == "tree" else O.DIRECT
+        be = _run("port", b, method, g.param("G"), g.param("eps"), 0.0, bool(ref["has_pe"]))
+        a = by_id(be.download().id, be.accel())
+        ar = by_id(ref["order_id"], ref["acc"])
+        assert rel_rms(a[:3], ar[:3]) <= 1e-6
+        assert be.times()["interactions"] == int(ref["interactions"])
+        if ref["has_pe"] and len(b) > 1:
+            assert abs(be.diagnostics()["pe"] / float(ref["pe"]) - 1) <= 1e-6
+
+
+@pytest.mark.parametrize("name", FORCE_FIXTURES)
+def test_reference_forces_vs_fp64(name):
+    """The reference's own accuracy against the FP64 direct sum, as its tests require."""
+    g = Golden(name)
+    b = g.inputs()
+    if len(b) < 2:
+        return
+    exact = O.direct_fp64(b, g.param("G"), g.param("eps"))
+    for c in g.cases():
+        ref = g.case(c)
+        a = by_id(ref["order_id"], ref["acc"])[:3]
+        e = rel_rms(a, by_id(b.id, exact[:3]))
+        theta = THETA.get(c, 0.0)
+        assert e <= (1e-5 if theta == 0.0 else 1e-2), (c, e)
+
+
+def test_port_kdk_diagnostics_vs_golden():
+    g = Golden("kdk_plummer2000")
+    b = g.inputs()
+    ref = g.case("out")
+    be = O.OracleBackend("port", 0)
+    be.upload(b)
+    G, eps, dt = g.param("G"), g.param("eps"), g.param("dt")
+    be.compute_forces(O.DIRECT, G, eps, 0.6, True)
+    be.kick(dt)
+    be.drift(dt)
+    be.compute_forces(O.DIRECT, G, eps, 0.6, True)
+    be.kick(dt)
+    d = be.diagnostics()
+    keys = ("mass", "ke", "pe", "px", "py", "pz", "lx", "ly", "lz", "cx", "cy", "cz")
+    got = np.array([d[k] for k in keys])
+    scale = np.abs(ref["diag"]).max()
+    np.testing.assert_allclose(got, ref["diag"], rtol=1e-6, atol=1e-9 * scale)
+    # The reference build contracts x += v h into an FMA; states differ in the last bit.
+    assert abs(be.exact_potential_energy(G, eps) / float(ref["exact_pe"]) - 1) <= 1e-9
+    dn = be.download()
+    assert np.array_equal(dn.id, ref["id"])
+    np.testing.assert_allclose(dn.x, ref["x"], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.skipif(not O.available("ref"), reason="reference sources not present: golden vectors pin the port")
+@pytest.mark.parametrize("n,seed,kind", [(20000, 3, "plummer"), (30000, 5, "disk"), (4000, 9, "cube")])
+def test_port_vs_live_reference(n, seed, kind):
+    b = {"plummer": lambda: S.plummer(n, seed, cut=20), "disk": lambda: S.disk(n, seed),
+         "cube": lambda: S.cube(n, seed)}[kind]()
+    p = _run("port", b, O.TREE, 1.0, 0.01, 0.6, True)
+    r = _run("ref", b, O.TREE, 1.0, 0.01, 0.6, True)
+    assert np.array_equal(p.keys(), r.keys())
+    assert np.array_equal(p.download().id, r.download().id)
+    pn, rn = p.nodes(), r.nodes()
+    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qzz"):
+        assert np.array_equal(pn[f], rn[f]), f
+    assert np.array_equal(p.groups(), r.groups())
+    assert p.times()["interactions"] == r.times()["interactions"]
+    assert rel_rms(p.accel()[:3], r.accel()[:3]) <= 1e-6
+
+
+def test_fp64_adjoint_matches_central_differences():
+    """The FP64 adjoint oracle against FP64 central finite differences (h = 1e-5)."""
+    b = S.plummer(48, 2, cut=10)
+    x0, v0 = b.pos64(), b.vel64()
+    m = b.m.astype(np.float64)
+    rng = np.random.Generator(np.random.PCG64(5))
+    xstar = x0 + rng.normal(0, 1e-3, x0.shape)
+    G, eps, dt, steps = 1.0, 0.05, 1e-3, 40
+    # Target: the trajectory of the perturbed initial positions.
+    xs = xstar.copy()
+    vs = v0.copy()
+    _, _, _, _ = O.adjoint_direct_fp64(xs, vs, m, G, eps, dt, steps, np.zeros_like(xs))
+    L, gx, gv, gm = O.adjoint_direct_fp64(x0, v0, m, G, eps, dt, steps, xstar)
+    h = 1e-5
+    for (arr, grad, idx) in [(x0, gx, (3, 1)), (x0, gx, (17, 2)), (v0, gv, (5, 0)), (v0, gv, (40, 2))]:
+        p = arr.copy(); p[idx] += h
+        q = arr.copy(); q[idx] -= h
+        args_p = (p, v0) if arr is x0 else (x0, p)
+        args_q = (q, v0) if arr is x0 else (x0, q)
+        fd = (O.loss_direct_fp64(*args_p, m, G, eps, dt, steps, xstar)
+              - O.loss_direct_fp64(*args_q, m, G, eps, dt, steps, xstar)) / (2 * h)
+        assert abs(fd - grad[idx]) <= 1e-6 * max(abs(fd), 1e-12) + 1e-12, (idx, fd, grad[idx])
+    for k in (0, 11, 30):
+        p = m.copy(); p[k] += h
+        q = m.copy(); q[k] -= h
+        fd = (O.loss_direct_fp64(x0, v0, p, G, eps, dt, steps, xstar)
+              - O.loss_direct_fp64(x0, v0, q, G, eps, dt, steps, xstar)) / (2 * h)
+        assert abs(fd - gm[k]) <= 1e-6 * max(abs(fd), 1e-12) + 1e-12, (k, fd, gm[k])
