@@ -1,0 +1,159 @@
+/* lettuce_gb300.h -- C ABI of the GB300 force-and-integrate engine for lettuce.
+ *
+ * The engine is a drop-in for the reference's CUDA backend (NotMaxwell/lettuce_simulate_physics,
+ * src/cuda_backend.cu) behind the reference's C++ interface `class Backend` (src/backend.hpp:89-141).
+ * Every entry point below names the Backend member or factory it replaces. The C++ adapter that
+ * implements `Backend` over this ABI is lettuce_simulate_physics_gb300/integration/gb300_backend.cpp.
+ *
+ * Conventions
+ *  - Every call returns an lg_status; on failure lg_last_error() holds a message for this thread.
+ *    LG_ERR_RUNTIME is the reference's std::runtime_error, LG_ERR_LOGIC its std::logic_error
+ *    (a call made in the wrong state, e.g. kick after build_tree without a force call).
+ *  - Pointers are host pointers to plain arrays; sizes are element counts.
+ *  - One engine = one device, one non-blocking stream. kick and drift are asynchronous; times,
+ *    diagnostics, download, body_costs and the force calls synchronise, as in the reference.
+ *  - Bodies cross the boundary as float32 (the reference's Bodies, src/bodies.hpp:7-10); inside,
+ *    positions are FP64 and the drift is FP64. download() rounds positions to float.
+ */
+#ifndef LETTUCE_GB300_H
+#define LETTUCE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    LG_OK = 0,
+    LG_ERR_RUNTIME = 1,     /* std::runtime_error in the reference */
+    LG_ERR_LOGIC = 2,       /* std::logic_error in the reference */
+    LG_ERR_ARG = 3,         /* invalid argument (null pointer, size mismatch) */
+    LG_ERR_UNAVAILABLE = 4  /* no usable device or no kernel image (make_cuda_backend -> nullptr) */
+} lg_status;
+
+enum { LG_DIRECT = 0, LG_TREE = 1 }; /* ForceMethod, src/backend.hpp:12 */
+
+typedef struct lg_engine lg_engine;
+
+/* ForceParams, src/backend.hpp:14-19. */
+typedef struct {
+    double G;
+    double eps;   /* Plummer softening: a = G m d / (|d|^2 + eps^2)^(3/2) */
+    double theta; /* tree opening angle */
+    int32_t method;
+    int32_t reserved;
+} lg_force_params;
+
+/* Diag, src/backend.hpp:31-39. */
+typedef struct {
+    double mass, ke, pe;
+    int32_t has_pe, reserved;
+    double px, py, pz;
+    double lx, ly, lz;
+    double cx, cy, cz;
+} lg_diag;
+
+/* PhaseTimes, src/backend.hpp:41-50 (milliseconds, measured with CUDA events). */
+typedef struct {
+    double force_ms, sort_ms, build_ms, walk_ms, step_ms;
+    uint64_t interactions;
+    double comm_ms, balance_ms;
+} lg_phase_times;
+
+/* MemoryNeed, src/backend.hpp:24-27. */
+typedef struct {
+    uint64_t device, host;
+} lg_memory_estimate;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lg_last_error(void);
+
+/* cuda_compiled(), src/backend.hpp:146: 1 (this library is the CUDA build). */
+int lg_compiled(void);
+/* cuda_device_count(), src/backend.hpp:148: visible devices, 0 without a driver. */
+int lg_device_count(void);
+
+/* make_cuda_backend(device, why), src/backend.hpp:145 and src/cuda_backend.cu:2026-2048.
+ * LG_ERR_UNAVAILABLE (message = why) when the device is missing or has no sm_103a image. Reads
+ * LETTUCE_CUDA_WALK=group|body and LETTUCE_CUDA_GROUP=<max bodies per walk group> (default 128, the
+ * reference CPU backend's group rule, src/cpu_backend.cpp:27), as the reference reads its walk
+ * settings at construction (src/cuda_backend.cu:1239-1254). */
+lg_status lg_create(int device, lg_engine** out);
+/* ~Backend(). */
+void lg_destroy(lg_engine* e);
+
+/* Backend::name(), src/backend.hpp:93: "cuda: <device> (sm_XY, N SMs, M GB), <walk>". */
+lg_status lg_name(const lg_engine* e, char* buf, size_t cap);
+
+/* Backend::upload(const Bodies&), src/backend.hpp:95. Accelerations are zeroed. */
+lg_status lg_upload(lg_engine* e, size_t n, const float* x, const float* y, const float* z, const float* vx,
+                    const float* vy, const float* vz, const float* m, const uint32_t* id);
+/* Number of resident bodies (Bodies::size() of the next download). */
+lg_status lg_size(const lg_engine* e, size_t* n);
+/* Backend::download(Bodies&), src/backend.hpp:97: current (possibly sorted) order, ids identify. */
+lg_status lg_download(lg_engine* e, float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m,
+                      uint32_t* id);
+
+/* Backend::compute_forces(p, potential), src/backend.hpp:102. */
+lg_status lg_compute_forces(lg_engine* e, const lg_force_params* p, int potential);
+/* Backend::kick(dt), src/backend.hpp:103: v += a dt. LG_ERR_LOGIC if the accelerations are stale. */
+lg_status lg_kick(lg_engine* e, double dt);
+/* Backend::drift(dt), src/backend.hpp:104: x += v dt, in FP64. */
+lg_status lg_drift(lg_engine* e, double dt);
+/* Backend::diagnostics(), src/backend.hpp:106: FP64 reductions over the FP64 state. */
+lg_status lg_diagnostics(lg_engine* e, lg_diag* out);
+/* Backend::exact_potential_energy(G, eps), src/backend.hpp:108: O(N^2) FP64 pair sum. */
+lg_status lg_exact_potential_energy(lg_engine* e, double G, double eps, double* out);
+/* Backend::times(), src/backend.hpp:110. */
+lg_status lg_times(lg_engine* e, lg_phase_times* out);
+
+/* Backend::local_bounds(), src/backend.hpp:115: lo[3], hi[3] of the current positions. */
+lg_status lg_local_bounds(lg_engine* e, float lo[3], float hi[3]);
+/* Backend::build_tree(p), src/backend.hpp:118: sort and build for the current positions;
+ * invalidates accelerations, potential and costs; no-op for the direct method. */
+lg_status lg_build_tree(lg_engine* e, const lg_force_params* p);
+/* Backend::compute_forces_with(p, potential, remote), src/backend.hpp:128-129, with an empty
+ * remote list (the MPI locally-essential-tree exchange is not part of this engine; nremote > 0
+ * returns LG_ERR_RUNTIME). LG_ERR_LOGIC for the tree method without a current tree. */
+lg_status lg_compute_forces_with(lg_engine* e, const lg_force_params* p, int potential, size_t nremote);
+/* Backend::memory_need(n, method), src/backend.hpp:131. */
+lg_status lg_memory_need(uint64_t n, int method, lg_memory_estimate* out);
+/* Backend::device_memory(free, total), src/backend.hpp:134-137; free includes what the engine holds. */
+lg_status lg_device_memory(lg_engine* e, uint64_t* free_bytes, uint64_t* total_bytes);
+/* Backend::body_costs(cost), src/backend.hpp:141: interactions per body of the last force call, in
+ * download order (sum == interactions). *valid = 0 when there is none (the reference returns false). */
+lg_status lg_body_costs(lg_engine* e, float* cost, size_t n, int* valid);
+
+/* ---- Extensions: no counterpart in the reference interface ------------------------------------ */
+
+/* Accelerations and potential in the current body order (the reference tests read them through
+ * kick(1) on zero velocities; this reads them directly). pot may be NULL. */
+lg_status lg_read_accel(lg_engine* e, float* ax, float* ay, float* az, float* pot);
+/* FP64 positions in the current body order. */
+lg_status lg_read_pos64(lg_engine* e, double* x, double* y, double* z);
+
+/* Tree introspection after build_tree: the sorted Morton keys (frame-0 keys), and the octree in
+ * the reference CPU backend's node order and layout (src/cpu_backend.cpp:35-43): per node
+ * lo, hi, first, nchild; moments cx, cy, cz, m, qxx, qxy, qxz, qyy, qyz, qzz, rcrit2 as floats;
+ * geometric centre and half side. Any output pointer may be NULL. */
+lg_status lg_tree_counts(lg_engine* e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth);
+lg_status lg_tree_keys(lg_engine* e, uint64_t* keys, size_t n);
+lg_status lg_tree_nodes(lg_engine* e, uint32_t* lohi_first_nchild, float* moments11, float* geo4, size_t nodes);
+/* Walk groups in the reference's order: box centre and half (float 6) and body range (u32 2). */
+lg_status lg_tree_groups(lg_engine* e, float* box6, uint32_t* lohi, size_t groups);
+
+/* Timing helpers on the engine's stream (CUDA events; slot 0..15). */
+lg_status lg_event_record(lg_engine* e, int slot);
+lg_status lg_event_elapsed(lg_engine* e, int slot_a, int slot_b, float* ms);
+lg_status lg_synchronize(lg_engine* e);
+/* Writes a device buffer larger than L2 on the engine's stream (cache flush between timed steps). */
+lg_status lg_flush_l2(lg_engine* e);
+/* Number of engine kernel launches issued so far (a counter kept by the host side). */
+lg_status lg_launch_count(const lg_engine* e, uint64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

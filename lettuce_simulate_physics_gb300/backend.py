@@ -1,0 +1,386 @@
+"""The reference's Backend interface (src/backend.hpp:89-148) over the engine's C ABI.
+
+This is the Python face of include/lettuce_gb300.h, shaped like the reference's C++ class so the
+parity tests read like the reference's own tests (tests/test_cuda_backend.cpp): the same method
+names, argument meaning and error behaviour. Errors map as the reference's do: std::logic_error ->
+LogicError, std::runtime_error -> RuntimeError, and make_cuda_backend returns (None, why) when no
+usable device exists.
+
+The library is the in-tree build (lettuce_simulate_physics_gb300/_build/liblettuce_gb300.so). There
+is no fallback: without it every call fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .bodies import Bodies
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liblettuce_gb300.so")
+
+LG_OK, LG_ERR_RUNTIME, LG_ERR_LOGIC, LG_ERR_ARG, LG_ERR_UNAVAILABLE = range(5)
+
+
+class LogicError(Exception):
+    """A call made in the wrong state (the reference's std::logic_error)."""
+
+
+class UnavailableError(RuntimeError):
+    """No usable CUDA device, or no sm_103a image for it."""
+
+
+class ForceMethod(enum.IntEnum):
+    direct = 0
+    tree = 1
+
+
+@dataclass
+class ForceParams:
+    G: float = 1.0
+    eps: float = 0.01
+    theta: float = 0.6
+    method: ForceMethod = ForceMethod.direct
+
+
+@dataclass
+class Diag:
+    mass: float = 0.0
+    ke: float = 0.0
+    pe: float = 0.0
+    has_pe: bool = False
+    px: float = 0.0
+    py: float = 0.0
+    pz: float = 0.0
+    lx: float = 0.0
+    ly: float = 0.0
+    lz: float = 0.0
+    cx: float = 0.0
+    cy: float = 0.0
+    cz: float = 0.0
+
+
+@dataclass
+class PhaseTimes:
+    force_ms: float = 0.0
+    sort_ms: float = 0.0
+    build_ms: float = 0.0
+    walk_ms: float = 0.0
+    step_ms: float = 0.0
+    interactions: int = 0
+    comm_ms: float = 0.0
+    balance_ms: float = 0.0
+
+
+@dataclass
+class Box3:
+    lo: tuple = (0.0, 0.0, 0.0)
+    hi: tuple = (0.0, 0.0, 0.0)
+
+
+@dataclass
+class MemoryNeed:
+    device: int = 0
+    host: int = 0
+
+
+class _CForceParams(C.Structure):
+    _fields_ = [("G", C.c_double), ("eps", C.c_double), ("theta", C.c_double), ("method", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class _CDiag(C.Structure):
+    _fields_ = [("mass", C.c_double), ("ke", C.c_double), ("pe", C.c_double), ("has_pe", C.c_int32),
+                ("reserved", C.c_int32)] + [(k, C.c_double) for k in ("px", "py", "pz", "lx", "ly", "lz",
+                                                                         "cx", "cy", "cz")]
+
+
+class _CTimes(C.Structure):
+    _fields_ = [("force_ms", C.c_double), ("sort_ms", C.c_double), ("build_ms", C.c_double),
+                ("walk_ms", C.c_double), ("step_ms", C.c_double), ("interactions", C.c_uint64),
+                ("comm_ms", C.c_double), ("balance_ms", C.c_double)]
+
+
+class _CMem(C.Structure):
+    _fields_ = [("device", C.c_uint64), ("host", C.c_uint64)]
+
+
+_f = C.POINTER(C.c_float)
+_u = C.POINTER(C.c_uint32)
+_d = C.POINTER(C.c_double)
+_lib_handle = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def _lib() -> C.CDLL:
+    global _lib_handle
+    if _lib_handle is not None:
+        return _lib_handle
+    if not os.path.isfile(LIB_PATH):
+        raise RuntimeError(f"engine library {LIB_PATH} is not built; run lettuce_simulate_physics_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    st = C.c_int
+    sigs = {
+        "lg_last_error": (C.c_char_p, []),
+        "lg_compiled": (C.c_int, []),
+        "lg_device_count": (C.c_int, []),
+        "lg_create": (st, [C.c_int, C.POINTER(vp)]),
+        "lg_destroy": (None, [vp]),
+        "lg_name": (st, [vp, C.c_char_p, C.c_size_t]),
+        "lg_upload": (st, [vp, C.c_size_t, _f, _f, _f, _f, _f, _f, _f, _u]),
+        "lg_size": (st, [vp, C.POINTER(C.c_size_t)]),
+        "lg_download": (st, [vp, _f, _f, _f, _f, _f, _f, _f, _u]),
+        "lg_compute_forces": (st, [vp, C.POINTER(_CForceParams), C.c_int]),
+        "lg_kick": (st, [vp, C.c_double]),
+        "lg_drift": (st, [vp, C.c_double]),
+        "lg_diagnostics": (st, [vp, C.POINTER(_CDiag)]),
+        "lg_exact_potential_energy": (st, [vp, C.c_double, C.c_double, _d]),
+        "lg_times": (st, [vp, C.POINTER(_CTimes)]),
+        "lg_local_bounds": (st, [vp, _f, _f]),
+        "lg_build_tree": (st, [vp, C.POINTER(_CForceParams)]),
+        "lg_compute_forces_with": (st, [vp, C.POINTER(_CForceParams), C.c_int, C.c_size_t]),
+        "lg_memory_need": (st, [C.c_uint64, C.c_int, C.POINTER(_CMem)]),
+        "lg_device_memory": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "lg_body_costs": (st, [vp, _f, C.c_size_t, C.POINTER(C.c_int)]),
+        "lg_read_accel": (st, [vp, _f, _f, _f, _f]),
+        "lg_read_pos64": (st, [vp, _d, _d, _d]),
+        "lg_tree_counts": (st, [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                                C.POINTER(C.c_int)]),
+        "lg_tree_keys": (st, [vp, C.POINTER(C.c_uint64), C.c_size_t]),
+        "lg_tree_nodes": (st, [vp, _u, _f, _f, C.c_size_t]),
+        "lg_tree_groups": (st, [vp, _f, _u, C.c_size_t]),
+        "lg_event_record": (st, [vp, C.c_int]),
+        "lg_event_elapsed": (st, [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+        "lg_synchronize": (st, [vp]),
+        "lg_flush_l2": (st, [vp]),
+        "lg_launch_count": (st, [vp, C.POINTER(C.c_uint64)]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib_handle = lib
+    return lib
+
+
+def last_error() -> str:
+    return _lib().lg_last_error().decode()
+
+
+def _check(status: int) -> None:
+    if status == LG_OK:
+        return
+    msg = last_error()
+    if status == LG_ERR_LOGIC:
+        raise LogicError(msg)
+    if status == LG_ERR_UNAVAILABLE:
+        raise UnavailableError(msg)
+    if status == LG_ERR_ARG:
+        raise ValueError(msg)
+    raise RuntimeError(msg)
+
+
+def _fp(a):
+    return a.ctypes.data_as(_f)
+
+
+def _up(a):
+    return a.ctypes.data_as(_u)
+
+
+def _cparams(p: ForceParams) -> _CForceParams:
+    return _CForceParams(float(p.G), float(p.eps), float(p.theta), int(p.method), 0)
+
+
+def cuda_compiled() -> bool:
+    return bool(_lib().lg_compiled())
+
+
+def cuda_device_count() -> int:
+    return int(_lib().lg_device_count())
+
+
+class CudaBackend:
+    """Backend (src/backend.hpp:89-141) on one GB300 through the engine's C ABI."""
+
+    def __init__(self, device: int = 0):
+        lib = _lib()
+        h = C.c_void_p()
+        _check(lib.lg_create(int(device), C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- Backend ----
+    def name(self) -> str:
+        buf = C.create_string_buffer(512)
+        _check(self._lib.lg_name(self._h, buf, 512))
+        return buf.value.decode()
+
+    def upload(self, b: Bodies) -> None:
+        _check(self._lib.lg_upload(self._h, len(b), _fp(b.x), _fp(b.y), _fp(b.z), _fp(b.vx), _fp(b.vy), _fp(b.vz),
+                                   _fp(b.m), _up(b.id)))
+
+    def size(self) -> int:
+        n = C.c_size_t()
+        _check(self._lib.lg_size(self._h, C.byref(n)))
+        return int(n.value)
+
+    def download(self) -> Bodies:
+        out = Bodies.empty(self.size())
+        _check(self._lib.lg_download(self._h, _fp(out.x), _fp(out.y), _fp(out.z), _fp(out.vx), _fp(out.vy),
+                                     _fp(out.vz), _fp(out.m), _up(out.id)))
+        return out
+
+    def compute_forces(self, p: ForceParams, potential: bool = False) -> None:
+        cp = _cparams(p)
+        _check(self._lib.lg_compute_forces(self._h, C.byref(cp), int(bool(potential))))
+
+    def kick(self, dt: float) -> None:
+        _check(self._lib.lg_kick(self._h, float(dt)))
+
+    def drift(self, dt: float) -> None:
+        _check(self._lib.lg_drift(self._h, float(dt)))
+
+    def diagnostics(self) -> Diag:
+        d = _CDiag()
+        _check(self._lib.lg_diagnostics(self._h, C.byref(d)))
+        return Diag(d.mass, d.ke, d.pe, bool(d.has_pe), d.px, d.py, d.pz, d.lx, d.ly, d.lz, d.cx, d.cy, d.cz)
+
+    def exact_potential_energy(self, G: float, eps: float) -> float:
+        out = C.c_double()
+        _check(self._lib.lg_exact_potential_energy(self._h, float(G), float(eps), C.byref(out)))
+        return float(out.value)
+
+    def times(self) -> PhaseTimes:
+        t = _CTimes()
+        _check(self._lib.lg_times(self._h, C.byref(t)))
+        return PhaseTimes(t.force_ms, t.sort_ms, t.build_ms, t.walk_ms, t.step_ms, int(t.interactions), t.comm_ms,
+                          t.balance_ms)
+
+    def local_bounds(self) -> Box3:
+        lo = np.zeros(3, np.float32)
+        hi = np.zeros(3, np.float32)
+        _check(self._lib.lg_local_bounds(self._h, _fp(lo), _fp(hi)))
+        return Box3(tuple(lo.tolist()), tuple(hi.tolist()))
+
+    def build_tree(self, p: ForceParams) -> None:
+        cp = _cparams(p)
+        _check(self._lib.lg_build_tree(self._h, C.byref(cp)))
+
+    def compute_forces_with(self, p: ForceParams, potential: bool = False, remote=()) -> None:
+        cp = _cparams(p)
+        _check(self._lib.lg_compute_forces_with(self._h, C.byref(cp), int(bool(potential)), len(remote)))
+
+    @staticmethod
+    def memory_need(n: int, method: ForceMethod) -> MemoryNeed:
+        m = _CMem()
+        _check(_lib().lg_memory_need(int(n), int(method), C.byref(m)))
+        return MemoryNeed(int(m.device), int(m.host))
+
+    def device_memory(self):
+        f = C.c_uint64()
+        t = C.c_uint64()
+        _check(self._lib.lg_device_memory(self._h, C.byref(f), C.byref(t)))
+        return True, int(f.value), int(t.value)
+
+    def body_costs(self):
+        n = self.size()
+        c = np.zeros(max(n, 1), np.float32)
+        valid = C.c_int()
+        _check(self._lib.lg_body_costs(self._h, _fp(c), n, C.byref(valid)))
+        return bool(valid.value), c[:n]
+
+    # ---- extensions ----
+    def accel(self) -> np.ndarray:
+        """(4, n) float32: ax, ay, az, phi in the current body order."""
+        n = self.size()
+        a = np.zeros((4, max(n, 1)), np.float32)
+        _check(self._lib.lg_read_accel(self._h, _fp(a[0]), _fp(a[1]), _fp(a[2]), _fp(a[3])))
+        return a[:, :n]
+
+    def pos64(self) -> np.ndarray:
+        n = self.size()
+        p = np.zeros((3, max(n, 1)), np.float64)
+        d = [p[k].ctypes.data_as(_d) for k in range(3)]
+        _check(self._lib.lg_read_pos64(self._h, *d))
+        return p[:, :n]
+
+    def tree_counts(self):
+        a, b, c, d = C.c_size_t(), C.c_size_t(), C.c_size_t(), C.c_int()
+        _check(self._lib.lg_tree_counts(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return dict(nodes=int(a.value), leaves=int(b.value), groups=int(c.value), max_depth=int(d.value))
+
+    def tree_keys(self) -> np.ndarray:
+        n = self.size()
+        k = np.zeros(max(n, 1), np.uint64)
+        _check(self._lib.lg_tree_keys(self._h, k.ctypes.data_as(C.POINTER(C.c_uint64)), n))
+        return k[:n]
+
+    def tree_nodes(self):
+        """Nodes in the reference CPU backend's order: (range (T,4) u32 lo/hi/first/nchild,
+        moments (T,11) f32 cx cy cz m qxx qxy qxz qyy qyz qzz rcrit2, geo (T,4) f32)."""
+        T = self.tree_counts()["nodes"]
+        r = np.zeros((T, 4), np.uint32)
+        mo = np.zeros((T, 11), np.float32)
+        g = np.zeros((T, 4), np.float32)
+        _check(self._lib.lg_tree_nodes(self._h, _up(r), _fp(mo), _fp(g), T))
+        return r, mo, g
+
+    def tree_groups(self):
+        G = self.tree_counts()["groups"]
+        box = np.zeros((G, 6), np.float32)
+        lohi = np.zeros((G, 2), np.uint32)
+        _check(self._lib.lg_tree_groups(self._h, _fp(box), _up(lohi), G))
+        return box, lohi
+
+    def event_record(self, slot: int) -> None:
+        _check(self._lib.lg_event_record(self._h, int(slot)))
+
+    def event_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        _check(self._lib.lg_event_elapsed(self._h, int(a), int(b), C.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        _check(self._lib.lg_synchronize(self._h))
+
+    def flush_l2(self) -> None:
+        _check(self._lib.lg_flush_l2(self._h))
+
+    def launch_count(self) -> int:
+        c = C.c_uint64()
+        _check(self._lib.lg_launch_count(self._h, C.byref(c)))
+        return int(c.value)
+
+
+def make_cuda_backend(device: int = 0):
+    """(backend, "") or (None, why), as make_cuda_backend(device, why) (src/backend.hpp:145)."""
+    try:
+        return CudaBackend(device), ""
+    except UnavailableError as e:
+        return None, str(e)

@@ -1,0 +1,228 @@
+// Direct summation (the reference's direct<POT>, src/cpu_backend.cpp:353-392, and direct_kernel,
+// src/cuda_backend.cu:301-350), GB300 form:
+//  - each thread keeps IPT i-bodies in registers;
+//  - j-bodies stream through shared memory in tiles of TILE float4 (hi x, hi y, hi z, m) plus the
+//    float4 low parts, fetched by the TMA engine (cp.async.bulk, mbarrier completion) into two
+//    stages, so the copy of tile t+2 overlaps the arithmetic on tile t;
+//  - each tile is converted once per block to coordinates relative to the block origin o (the
+//    first i-body): (x_hi - o_hi) + (x_lo - o_lo) in FP32, so close pairs keep the FP64
+//    separation and the inner loop is plain FP32 (3 FADD, 3 FFMA, 1 MUFU.RSQ, 3 FMUL, 3 FFMA);
+//  - per-tile partial sums are added to the running sums with Kahan compensation;
+//  - small N splits the j range over blockIdx.y (split-j); the slices' partials are summed in a
+//    fixed order by a second kernel, so results do not depend on scheduling.
+// Self interaction: with eps > 0 the self pair has d = 0 exactly (same relative coordinates), so
+// it adds nothing to a; its potential term m_i/eps is subtracted at the end. With eps == 0 the
+// r2 > 0 guard drops self and coincident pairs, as the reference does.
+#include "lg_engine.cuh"
+
+namespace lg {
+
+namespace {
+
+constexpr int DBS = 256;   // threads per block
+constexpr int TILE = 256;  // j-bodies per stage
+
+struct alignas(16) DirectSmem {
+    float4 raw_hm[2][TILE];
+    float4 raw_lo[2][TILE];
+    float4 rel[2][TILE];
+    uint64_t bar[2];
+};
+
+template <int IPT, bool POT, bool EPS0>
+__global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
+                                                int jslice, float G, float e2, float4* __restrict__ out, int write_final,
+                                                unsigned* err) {
+    __shared__ DirectSmem sm;
+    const int tid = threadIdx.x;
+    const int base = blockIdx.x * (DBS * IPT);
+    const int j0 = blockIdx.y * jslice;
+    const int j1 = min(n, j0 + jslice);
+    const int ntiles = (j1 - j0 + TILE - 1) / TILE;
+
+    // Block origin: the first i-body of the block.
+    const float4 oh = hm[base];
+    const float4 ol = lo[base];
+
+    float xi[IPT], yi[IPT], zi[IPT], mself[IPT];
+    float sx[IPT], sy[IPT], sz[IPT], sp[IPT], cx[IPT], cy[IPT], cz[IPT], cp[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        const int i = min(base + u * DBS + tid, n - 1);
+        const float4 h = hm[i], l = lo[i];
+        xi[u] = (h.x - oh.x) + (l.x - ol.x);
+        yi[u] = (h.y - oh.y) + (l.y - ol.y);
+        zi[u] = (h.z - oh.z) + (l.z - ol.z);
+        mself[u] = h.w;
+        sx[u] = sy[u] = sz[u] = sp[u] = 0.f;
+        cx[u] = cy[u] = cz[u] = cp[u] = 0.f;
+    }
+
+    if (tid == 0) {
+        mbar_init(&sm.bar[0], 1);
+        mbar_init(&sm.bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t) {
+        const int jt = j0 + t * TILE;
+        const unsigned cnt = static_cast<unsigned>(min(TILE, j1 - jt));
+        const int buf = t & 1;
+        mbar_arrive_expect_tx(&sm.bar[buf], 2u * cnt * 16u);
+        bulk_g2s(sm.raw_hm[buf], hm + jt, cnt * 16u, &sm.bar[buf]);
+        bulk_g2s(sm.raw_lo[buf], lo + jt, cnt * 16u, &sm.bar[buf]);
+    };
+    if (tid == 0) {
+        if (ntiles > 0) issue(0);
+        if (ntiles > 1) issue(1);
+    }
+
+    bool failed = false;
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int buf = t & 1;
+        const unsigned parity = (t >> 1) & 1;
+        const bool ok = mbar_wait_bounded(&sm.bar[buf], parity);
+        const int cnt = min(TILE, j1 - (j0 + t * TILE));
+        const int cnt8 = (cnt + 7) & ~7;
+        if (ok) {
+            for (int k = tid; k < cnt8; k += DBS) {
+                float4 r;
+                if (k < cnt) {
+                    const float4 h = sm.raw_hm[buf][k], l = sm.raw_lo[buf][k];
+                    r = make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
+                                    (h.z - oh.z) + (l.z - ol.z), h.w);
+                } else {
+                    r = make_float4(0.f, 0.f, 0.f, 0.f);  // zero mass at the origin adds nothing
+                }
+                sm.rel[buf][k] = r;
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0 && t + 2 < ntiles) {
+            fence_proxy_async_smem();
+            issue(t + 2);
+        }
+        float px[IPT], py[IPT], pz[IPT], pp[IPT];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) px[u] = py[u] = pz[u] = pp[u] = 0.f;
+        const float4* rel = sm.rel[buf];
+#pragma unroll 4
+        for (int k = 0; k < cnt8; ++k) {
+            const float4 q = rel[k];
+#pragma unroll
+            for (int u = 0; u < IPT; ++u) {
+                const float dx = q.x - xi[u], dy = q.y - yi[u], dz = q.z - zi[u];
+                const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
+                float inv = rsqrt_mufu(r2);
+                if (EPS0) inv = r2 > 0.f ? inv : 0.f;
+                const float mi = q.w * inv;
+                const float f = mi * (inv * inv);
+                px[u] = __fmaf_rn(f, dx, px[u]);
+                py[u] = __fmaf_rn(f, dy, py[u]);
+                pz[u] = __fmaf_rn(f, dz, pz[u]);
+                if (POT) pp[u] += mi;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            kahan_add(sx[u], cx[u], px[u]);
+            kahan_add(sy[u], cy[u], py[u]);
+            kahan_add(sz[u], cz[u], pz[u]);
+            if (POT) kahan_add(sp[u], cp[u], pp[u]);
+        }
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(err, kErrWaitTimeout);
+            // Let any copy still in flight land before the block's shared memory is released.
+            for (int u = t; u < min(ntiles, t + 2); ++u) mbar_wait_bounded(&sm.bar[u & 1], (u >> 1) & 1);
+        }
+        return;
+    }
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        const int i = base + u * DBS + tid;
+        if (i >= n) continue;
+        float p = sp[u] - cp[u];
+        if (POT && !EPS0 && i >= j0 && i < j1) {
+            // The self pair's potential term, exactly as the loop formed it (r2 == e2).
+            p -= mself[u] * rsqrt_mufu(e2);
+        }
+        if (write_final)
+            out[i] = make_float4(G * (sx[u] - cx[u]), G * (sy[u] - cy[u]), G * (sz[u] - cz[u]), POT ? -G * p : 0.f);
+        else
+            out[static_cast<size_t>(blockIdx.y) * n + i] =
+                make_float4(sx[u] - cx[u], sy[u] - cy[u], sz[u] - cz[u], POT ? p : 0.f);
+    }
+}
+
+// Sums the split-j partials in slice order (Kahan) and scales by G.
+__global__ void k_direct_reduce(const float4* __restrict__ partial, int n, int slices, float G, float4* __restrict__ acc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
+    for (int k = 0; k < slices; ++k) {
+        const float4 p = partial[static_cast<size_t>(k) * n + i];
+        kahan_add(s[0], c[0], p.x);
+        kahan_add(s[1], c[1], p.y);
+        kahan_add(s[2], c[2], p.z);
+        kahan_add(s[3], c[3], p.w);
+    }
+    acc[i] = make_float4(G * (s[0] - c[0]), G * (s[1] - c[1]), G * (s[2] - c[2]), -G * (s[3] - c[3]));
+}
+
+template <int IPT>
+void launch_ipt(const BodyArrays b, int n, float G, float e2, bool pot, bool eps0, int jslice, int slices, float4* out,
+                int write_final, unsigned* err, cudaStream_t s) {
+    dim3 grid((n + DBS * IPT - 1) / (DBS * IPT), slices);
+    if (pot) {
+        if (eps0) k_direct<IPT, true, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+        else k_direct<IPT, true, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+    } else {
+        if (eps0) k_direct<IPT, false, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+        else k_direct<IPT, false, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+    }
+    LG_LAUNCHED();
+}
+
+}  // namespace
+
+DirectShape default_direct_shape(int n, int sms) {
+    DirectShape sh;
+    sh.ipt = n >= 8 * 1024 ? 4 : (n >= 2048 ? 2 : 1);
+    sh.tile = TILE;
+    const int iblocks = (n + DBS * sh.ipt - 1) / (DBS * sh.ipt);
+    const int target = 3 * sms;  // about three resident blocks per SM
+    const int max_slices = (n + TILE - 1) / TILE;
+    int slices = (target + iblocks - 1) / iblocks;
+    slices = slices < 1 ? 1 : (slices > max_slices ? max_slices : slices);
+    sh.slices = slices;
+    return sh;
+}
+
+void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential, bool eps0, const DirectShape& shape,
+                   float4* acc, float4* partial, unsigned* err, cudaStream_t s) {
+    if (n <= 0) return;
+    int slices = shape.slices < 1 ? 1 : shape.slices;
+    int jslice = (n + slices - 1) / slices;
+    jslice = (jslice + TILE - 1) / TILE * TILE;
+    slices = (n + jslice - 1) / jslice;
+    const bool final_out = slices == 1;
+    float4* out = final_out ? acc : partial;
+    switch (shape.ipt) {
+        case 1: launch_ipt<1>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
+        case 2: launch_ipt<2>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
+        case 8: launch_ipt<8>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
+        default: launch_ipt<4>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
+    }
+    if (!final_out) {
+        k_direct_reduce<<<(n + 255) / 256, 256, 0, s>>>(partial, n, slices, G, acc);
+        LG_LAUNCHED();
+    }
+}
+
+}  // namespace lg

@@ -1,0 +1,116 @@
+// The engine object behind the C ABI, and the tree stages it calls.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+
+#include "../../include/lettuce_gb300.h"
+#include "lg_engine.cuh"
+
+namespace lg {
+
+struct TreeState;  // tree.cu
+
+// Read-only view of the built tree for the walk.
+struct TreeView {
+    const uint4* nd_range;    // (lo, hi, first, nchild), reference node order
+    const float4* nd_com;     // (cx, cy, cz, m)
+    const float4* nd_comlo;   // low parts of the FP64 centre of mass
+    const float4* nd_q0;      // (qxx, qxy, qxz, qyy)
+    const float4* nd_q1;      // (qyz, qzz, rcrit2, 0)
+    const uint2* grp_range;   // walk groups (lo, hi), reference order
+    const float4* grp_box;    // 2 per group: (bx, by, bz, 0), (hx, hy, hz, 0)
+    const unsigned* ngroups;  // device-side group count
+    size_t T;
+};
+
+struct BodySet {
+    DevBuf x, y, z, hm, lo, vx, vy, vz, m, cost, id;
+};
+
+struct Engine {
+    explicit Engine(int device);
+    ~Engine();
+
+    // Backend semantics (src/backend.hpp:89-141).
+    void upload(size_t count, const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                const float* vz, const float* m, const uint32_t* id);
+    void download(float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m, uint32_t* id);
+    void build_tree(const lg_force_params& p);
+    void compute_forces_with(const lg_force_params& p, bool potential, size_t nremote);
+    void kick(double dt);
+    void drift(double dt);
+    lg_diag diagnostics();
+    double exact_potential_energy(double G, double eps);
+    lg_phase_times get_times();
+    void local_bounds(float lo[3], float hi[3]);
+    bool body_costs(float* cost, size_t count);
+    void read_accel(float* ax, float* ay, float* az, float* pot);
+    void read_pos64(double* x, double* y, double* z);
+    void flush_l2();
+    size_t held_bytes() const;
+
+    BodyArrays bodies(int which) const;
+    void reserve_bodies(size_t count);
+    unsigned* err_word() const;
+    unsigned* ticket() const;
+    unsigned long long* inter_counter() const;
+    double* dscratch() const;
+    float elapsed(int a, int b) const;
+    void check_device_errors(const char* where);
+
+    // Device, stream, events.
+    int dev = 0;
+    int sms = 0;
+    int l2_bytes = 0;
+    std::string name;
+    cudaStream_t stream = nullptr;
+    enum { EV_BUILD0, EV_SORTED, EV_BUILT, EV_WALK0, EV_WALK1, EV_KICK0, EV_KICK1, EV_DRIFT0, EV_DRIFT1, EV_COUNT };
+    cudaEvent_t events[EV_COUNT] = {};
+    static constexpr int kUserEvents = 16;
+    cudaEvent_t user_events[kUserEvents] = {};
+
+    // Walk settings (LETTUCE_CUDA_WALK / LETTUCE_CUDA_GROUP).
+    bool walk_body = false;
+    int group_max = 128;
+    DirectShape direct_shape_override{0, 0, 0};
+
+    // State.
+    int n = 0;
+    int cur = 0;  // which BodySet holds the current bodies
+    BodySet set[2];
+    DevBuf acc;          // float4 per body
+    DevBuf staging;      // 3 floats per body for upload/download
+    DevBuf partial;      // split-j partial sums (scratch)
+    DevBuf diag_partial; // per-block FP64 partials
+    DevBuf flush_buf;
+    DevBuf walk_stack;   // per-warp traversal stacks of the tree walk
+    DevBuf small;        // error word, tickets, counters, FP64 results
+    unsigned* pinned_small = nullptr;
+    bool has_pe = false, acc_ok = true, tree_ok = false, costs_ok = false;
+    bool kick_rec = false, drift_rec = false, pend_tree_times = false;
+    lg_phase_times times{};
+    uint64_t launches = 0;
+    std::unique_ptr<TreeState, void (*)(TreeState*)> tree{nullptr, nullptr};
+};
+
+extern thread_local std::string g_last_error;
+
+// tree.cu
+std::unique_ptr<TreeState, void (*)(TreeState*)> make_tree_state();
+void tree_sort(Engine& e);                    // keys, radix sort, permute (+ key restarts)
+void tree_build(Engine& e, double theta);     // octree, groups, moments
+size_t tree_held_bytes(const Engine& e);
+TreeView tree_view(Engine& e);
+void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth);
+void tree_keys(Engine& e, uint64_t* keys, size_t n);
+void tree_nodes(Engine& e, uint32_t* lohi_first_nchild, float* moments11, float* geo4, size_t nodes);
+void tree_groups(Engine& e, float* box6, uint32_t* lohi, size_t groups);
+lg_memory_estimate memory_need(uint64_t n, int method);
+const void* probe_kernel();
+// walk.cu
+void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0);
+
+}  // namespace lg

@@ -1,0 +1,281 @@
+// Integration and reduction kernels: upload widening, download rounding, FP32 kick, FP64 drift,
+// FP64 diagnostics and bounds, the exact FP64 potential energy, and utility kernels.
+#include "lg_engine.cuh"
+
+namespace lg {
+
+namespace {
+
+constexpr int BS = 256;
+
+inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
+
+// hi = nearest float, lo = nearest float to the remainder (exact in double).
+__device__ __forceinline__ void split_hilo(double v, float& hi, float& lo) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(__dsub_rn(v, static_cast<double>(hi)));
+}
+
+__device__ __forceinline__ void store_hilo(BodyArrays b, int i, double x, double y, double z, float m) {
+    float hx, hy, hz, lx, ly, lz;
+    split_hilo(x, hx, lx);
+    split_hilo(y, hy, ly);
+    split_hilo(z, hz, lz);
+    b.hm[i] = make_float4(hx, hy, hz, m);
+    b.lo[i] = make_float4(lx, ly, lz, 0.f);
+}
+
+// upload: float positions widen exactly to double (src/backend.hpp:95 semantics, FP64 inside).
+__global__ void k_widen(const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ z,
+                        const float* __restrict__ m, BodyArrays b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double px = x[i], py = y[i], pz = z[i];
+    b.x[i] = px;
+    b.y[i] = py;
+    b.z[i] = pz;
+    store_hilo(b, i, px, py, pz, m[i]);
+}
+
+__global__ void k_round_pos(const BodyArrays b, float* __restrict__ x, float* __restrict__ y, float* __restrict__ z,
+                            int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = __double2float_rn(b.x[i]);
+    y[i] = __double2float_rn(b.y[i]);
+    z[i] = __double2float_rn(b.z[i]);
+}
+
+// v += a dt in FP32 (src/cpu_backend.cpp:279-290).
+__global__ void k_kick(BodyArrays b, const float4* __restrict__ acc, float dt, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 a = acc[i];
+    b.vx[i] = __fmaf_rn(a.x, dt, b.vx[i]);
+    b.vy[i] = __fmaf_rn(a.y, dt, b.vy[i]);
+    b.vz[i] = __fmaf_rn(a.z, dt, b.vz[i]);
+}
+
+// x += v dt in FP64, then the hi/lo split the force kernels read.
+__global__ void k_drift(BodyArrays b, double dt, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double px = __fma_rn(static_cast<double>(b.vx[i]), dt, b.x[i]);
+    double py = __fma_rn(static_cast<double>(b.vy[i]), dt, b.y[i]);
+    double pz = __fma_rn(static_cast<double>(b.vz[i]), dt, b.z[i]);
+    b.x[i] = px;
+    b.y[i] = py;
+    b.z[i] = pz;
+    store_hilo(b, i, px, py, pz, b.m[i]);
+}
+
+constexpr int NDIAG = 12;
+
+// Block-level FP64 sum of NDIAG values in a fixed order (warp shuffles, then warps in order).
+__device__ void block_sum(double (&v)[NDIAG], double* sh /* [BS/32][NDIAG] */) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NDIAG; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NDIAG; ++k) sh[w * NDIAG + k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NDIAG; ++k) {
+            double s = 0;
+            for (int u = 0; u < BS / 32; ++u) s += sh[u * NDIAG + k];
+            v[k] = s;
+        }
+    }
+}
+
+// Diagnostics (src/cpu_backend.cpp:307-329) over the FP64 state: per-block partials, the last
+// block to finish sums them in block order (deterministic).
+__global__ void k_diag(const BodyArrays b, const float4* __restrict__ acc, int n, double* partial, unsigned* ticket,
+                       double* out) {
+    __shared__ double sh[(BS / 32) * NDIAG];
+    __shared__ bool last;
+    double v[NDIAG] = {};
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+        double m = b.m[i], x = b.x[i], y = b.y[i], z = b.z[i];
+        double vx = b.vx[i], vy = b.vy[i], vz = b.vz[i];
+        v[0] += m;
+        v[1] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        v[2] += m * static_cast<double>(acc[i].w);
+        v[3] += m * vx;
+        v[4] += m * vy;
+        v[5] += m * vz;
+        v[6] += m * (y * vz - z * vy);
+        v[7] += m * (z * vx - x * vz);
+        v[8] += m * (x * vy - y * vx);
+        v[9] += m * x;
+        v[10] += m * y;
+        v[11] += m * z;
+    }
+    block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NDIAG; ++k) partial[blockIdx.x * NDIAG + k] = v[k];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x < NDIAG) {
+        __threadfence();
+        double s = 0;
+        for (int blk = 0; blk < static_cast<int>(gridDim.x); ++blk) s += __ldcg(&partial[blk * NDIAG + threadIdx.x]);
+        out[threadIdx.x] = s;
+        if (threadIdx.x == 0) *ticket = 0;
+    }
+}
+
+// Bounding box of the FP64 positions: out6 = min xyz, max xyz.
+__global__ void k_bounds(const BodyArrays b, int n, double* partial, unsigned* ticket, double* out6) {
+    __shared__ double sh[6][BS / 32];
+    __shared__ bool last;
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+        double p[3] = {b.x[i], b.y[i], b.z[i]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fmin(v[c], p[c]);
+            v[3 + c] = fmax(v[3 + c], p[c]);
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            double t = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
+        }
+        if (lane == 0) sh[c][w] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        double r = sh[c][0];
+        for (int u = 1; u < BS / 32; ++u) r = c < 3 ? fmin(r, sh[c][u]) : fmax(r, sh[c][u]);
+        partial[blockIdx.x * 6 + c] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x < 6) {
+        __threadfence();
+        const int c = threadIdx.x;
+        double r = __ldcg(&partial[c]);
+        for (int blk = 1; blk < static_cast<int>(gridDim.x); ++blk) {
+            double t = __ldcg(&partial[blk * 6 + c]);
+            r = c < 3 ? fmin(r, t) : fmax(r, t);
+        }
+        out6[c] = r;
+        if (c == 0) *ticket = 0;
+    }
+}
+
+// Exact potential energy (src/cpu_backend.cpp:331-347): sum over i<j of m_i m_j / sqrt(r^2+eps^2)
+// in FP64 from the FP64 positions; one block per 256 i-bodies, j tiled through shared memory.
+__global__ void k_exact_pe(const BodyArrays b, int n, double e2, double* out) {
+    __shared__ double sx[BS], sy[BS], sz[BS], sm[BS];
+    __shared__ double red[BS / 32];
+    const int i = blockIdx.x * BS + threadIdx.x;
+    double xi = 0, yi = 0, zi = 0, mi = 0;
+    if (i < n) { xi = b.x[i]; yi = b.y[i]; zi = b.z[i]; mi = b.m[i]; }
+    double s = 0;
+    // Only tiles that can hold j > i for some i of this block.
+    for (int j0 = blockIdx.x * BS; j0 < n; j0 += BS) {
+        const int j = j0 + threadIdx.x;
+        __syncthreads();
+        if (j < n) { sx[threadIdx.x] = b.x[j]; sy[threadIdx.x] = b.y[j]; sz[threadIdx.x] = b.z[j]; sm[threadIdx.x] = b.m[j]; }
+        __syncthreads();
+        const int cnt = min(BS, n - j0);
+        if (i < n) {
+            for (int k = 0; k < cnt; ++k) {
+                if (j0 + k <= i) continue;
+                double dx = sx[k] - xi, dy = sy[k] - yi, dz = sz[k] - zi;
+                double r2 = dx * dx + dy * dy + dz * dz + e2;
+                if (r2 > 0) s += sm[k] / sqrt(r2);
+            }
+        }
+    }
+    s *= mi;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int u = 0; u < BS / 32; ++u) t += red[u];
+        atomicAdd(out, t);
+    }
+}
+
+__global__ void k_fill(float* __restrict__ a, float v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+__global__ void k_flush(float* __restrict__ a, size_t count) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        a[i] = a[i] * 0.5f + 1.f;
+}
+
+}  // namespace
+
+void launch_widen(const float* x, const float* y, const float* z, const float* m, BodyArrays b, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_widen<<<grid_for(n, BS), BS, 0, s>>>(x, y, z, m, b, n);
+    LG_LAUNCHED();
+}
+
+void launch_round_pos(const BodyArrays b, float* x, float* y, float* z, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_round_pos<<<grid_for(n, BS), BS, 0, s>>>(b, x, y, z, n);
+    LG_LAUNCHED();
+}
+
+void launch_kick(BodyArrays b, const float4* acc, float dt, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_kick<<<grid_for(n, BS), BS, 0, s>>>(b, acc, dt, n);
+    LG_LAUNCHED();
+}
+
+void launch_drift(BodyArrays b, double dt, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_drift<<<grid_for(n, BS), BS, 0, s>>>(b, dt, n);
+    LG_LAUNCHED();
+}
+
+void launch_diag(const BodyArrays b, const float4* acc, int n, double* partial, unsigned* ticket, double* out,
+                 int blocks, cudaStream_t s) {
+    k_diag<<<blocks, BS, 0, s>>>(b, acc, n, partial, ticket, out);
+    LG_LAUNCHED();
+}
+
+void launch_bounds(const BodyArrays b, int n, double* partial, unsigned* ticket, double* out6, int blocks,
+                   cudaStream_t s) {
+    k_bounds<<<blocks, BS, 0, s>>>(b, n, partial, ticket, out6);
+    LG_LAUNCHED();
+}
+
+void launch_exact_pe(const BodyArrays b, int n, double e2, double* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_exact_pe<<<grid_for(n, BS), BS, 0, s>>>(b, n, e2, out);
+    LG_LAUNCHED();
+}
+
+void launch_fill_cost(float* cost, float v, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_fill<<<grid_for(n, BS), BS, 0, s>>>(cost, v, n);
+    LG_LAUNCHED();
+}
+
+void launch_flush(float* buf, size_t count, cudaStream_t s) {
+    k_flush<<<1024, BS, 0, s>>>(buf, count);
+    LG_LAUNCHED();
+}
+
+}  // namespace lg

@@ -1,0 +1,1257 @@
+// Tree build for the Barnes-Hut method: Morton keys, onesweep LSD radix sort, permute, key
+// restarts, the octree in the reference CPU backend's exact topology and node order, walk groups,
+// and the FP64 bottom-up upsweep of monopole and quadrupole moments.
+//
+// Parity target: the reference CPU backend (src/cpu_backend.cpp:395-664). After an upload (FP64
+// positions equal to the float inputs) the keys, the sort permutation, the node array (lo, hi,
+// first, nchild in the same indices), the cell geometry and the groups are bit-identical to the
+// reference's; the moments use the reference's FP64 operation order without contraction.
+//
+// Construction (no level-by-level loop, no recursion):
+//  1. bbox and key frame (FP64), keys (src/cpu_backend.cpp:418-428 formula), identity values.
+//  2. Onesweep radix sort (Adinets & Merrill 2022): one histogram pass for all eight 8-bit digits,
+//     then one kernel per digit with decoupled look-back across tiles; digits that are constant
+//     over all keys are skipped on the device. Stable, so the permutation equals the reference's.
+//  3. Key restarts: runs of > 16 identical keys are re-keyed in their own bounding cube (the
+//     reference's rekey, src/cpu_backend.cpp:503-530) and sorted by (key, restart key).
+//  4. Leaves from key windows: body i's leaf depth is 1 + the deepest common octal prefix of any
+//     window of LEAF_MAX+1 consecutive sorted keys that contains i (the first depth at which its
+//     cell holds <= LEAF_MAX bodies); group depth likewise with windows of group_max+1.
+//  5. Octree nodes in pre-order, enumerated per leaf: leaf l owns the ancestors at depths
+//     c+1 .. depth-1, c = common prefix with the previous leaf (Karras 2012's adjacent-key rule in
+//     octree form). A scan gives every node's pre-order index; body ranges, parents and children
+//     follow from binary searches over the sorted keys.
+//  6. Node indices of the reference (children contiguous, child blocks in parent pre-order):
+//     first child of v = 1 + exclusive scan of nchild over pre-order.
+//  7. Upsweep: one thread per leaf computes its FP64 moments, then climbs; at each parent the
+//     last-arriving child (atomic counter) combines all children in index order, so the result
+//     does not depend on arrival order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace lg {
+
+namespace {
+
+constexpr int LEAF_MAX = 16;   // src/cpu_backend.cpp:24
+constexpr int MAX_LEVEL = 21;  // :28
+constexpr int MAX_DEPTH = 2 * MAX_LEVEL;  // frame 0 plus one key restart
+constexpr int BS = 256;
+
+inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
+
+// ---- sort control --------------------------------------------------------------------------
+constexpr int RADIX = 256;
+constexpr int PASSES = 8;
+constexpr int SORT_BS = 256;
+constexpr int SORT_IPT = 16;
+constexpr int SORT_TILE = SORT_BS * SORT_IPT;
+constexpr unsigned FLAG_AGG = 1u << 30, FLAG_INC = 2u << 30, VAL_MASK = (1u << 30) - 1;
+
+struct SortCtl {
+    unsigned sel;
+    unsigned skip[PASSES];
+    unsigned tile_ctr[PASSES];
+    unsigned done_ctr[PASSES];
+};
+
+}  // namespace
+
+struct TreeState {
+    // sort
+    DevBuf keysA, keysB, valsA, valsB, hist, lookback, ctl;
+    // sorted keys (frame 0 and restart keys), per-body tree data
+    DevBuf skey, skey1, key1tmp, runid, bdepth, flag, leafid;
+    // frame and key-restart runs
+    DevBuf frame, runs, runcube, counts;
+    // leaves
+    DevBuf leaf_first, leaf_depth, leaf_c, leaf_pre, leaf_node;
+    // pre-order nodes
+    DevBuf pn_lohi, pn_meta, pn_nchild, pn_cb, pn_cpu;
+    // reference-order nodes
+    DevBuf nd_range, nd_com, nd_comlo, nd_q0, nd_q1, nd_geo, nd_parent, nd_arrive;
+    // groups
+    DevBuf gflag, gidx, grp_node, grp_range, grp_box, leaf_cnt;
+    // scan state
+    DevBuf scan_state, scan_ctr;
+    size_t K = 0, T = 0, ngroups = 0, nruns = 0;
+    int max_depth = 0;
+    bool restarted = false;
+    int group_max = 128;
+};
+
+namespace {
+
+void destroy_tree(TreeState* t) { delete t; }
+
+// ---- device helpers --------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t spread21(uint64_t v) {
+    v &= 0x1fffffULL;
+    v = (v | v << 32) & 0x1f00000000ffffULL;
+    v = (v | v << 16) & 0x1f0000ff0000ffULL;
+    v = (v | v << 8) & 0x100f00f00f00f00fULL;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+    v = (v | v << 2) & 0x1249249249249249ULL;
+    return v;
+}
+
+// Quantised coordinate of src/cpu_backend.cpp:423: uint64(clamp((v - o) * s, 0, lim)), FP64,
+// round-to-nearest products, truncation.
+__device__ __forceinline__ uint64_t quantize(double v, double o, double s, double lim) {
+    double q = __dmul_rn(__dsub_rn(v, o), s);
+    q = fmin(fmax(q, 0.0), lim);
+    return static_cast<uint64_t>(__double2ull_rz(q));
+}
+
+__device__ __forceinline__ uint64_t morton(double x, double y, double z, double ox, double oy, double oz, double s) {
+    const double lim = static_cast<double>((1u << MAX_LEVEL) - 1);
+    return spread21(quantize(x, ox, s, lim)) << 2 | spread21(quantize(y, oy, s, lim)) << 1 |
+           spread21(quantize(z, oz, s, lim));
+}
+
+// Common octal prefix (0..21) of two 63-bit keys.
+__device__ __forceinline__ int cpl21(uint64_t a, uint64_t b) { return (__clzll(a ^ b) - 1) / 3; }
+
+// Common octal prefix (0..42) of composite keys (key, restart key).
+__device__ __forceinline__ int cpl42(const uint64_t* k0, const uint64_t* k1, int i, int j) {
+    const uint64_t a = k0[i], b = k0[j];
+    if (a != b || !k1) return cpl21(a, b);
+    return MAX_LEVEL + cpl21(k1[i], k1[j]);
+}
+
+// Octal digit of composite key at depth d (1-based).
+__device__ __forceinline__ int digit_at(const uint64_t* k0, const uint64_t* k1, int i, int d) {
+    if (d <= MAX_LEVEL) return static_cast<int>((k0[i] >> (3 * (MAX_LEVEL - d))) & 7);
+    return static_cast<int>((k1[i] >> (3 * (2 * MAX_LEVEL - d))) & 7);
+}
+
+// ---- frame and keys --------------------------------------------------------------------------
+// frame: [0..2] origin, [3] side, [4] scale 2^21/side.
+__global__ void k_frame(const BodyArrays b, int n, double* partial, unsigned* ticket, double* frame) {
+    __shared__ double sh[6][BS / 32];
+    __shared__ bool last;
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
+        double p[3] = {b.x[i], b.y[i], b.z[i]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fmin(v[c], p[c]);
+            v[3 + c] = fmax(v[3 + c], p[c]);
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            double t = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
+        }
+        if (lane == 0) sh[c][w] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        double r = sh[c][0];
+        for (int u = 1; u < BS / 32; ++u) r = c < 3 ? fmin(r, sh[c][u]) : fmax(r, sh[c][u]);
+        partial[blockIdx.x * 6 + c] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double r[6];
+        for (int c = 0; c < 6; ++c) r[c] = __ldcg(&partial[c]);
+        for (int blk = 1; blk < static_cast<int>(gridDim.x); ++blk)
+            for (int c = 0; c < 6; ++c) {
+                double t = __ldcg(&partial[blk * 6 + c]);
+                r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
+            }
+        // src/cpu_backend.cpp:404-406: side = max extent, widened by 1e-6; 1 if all coincide.
+        double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
+        side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
+        frame[0] = r[0];
+        frame[1] = r[1];
+        frame[2] = r[2];
+        frame[3] = side;
+        frame[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
+        *ticket = 0;
+    }
+}
+
+__global__ void k_keys(const BodyArrays b, int n, const double* __restrict__ frame, uint64_t* __restrict__ keys,
+                       uint32_t* __restrict__ vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = morton(b.x[i], b.y[i], b.z[i], frame[0], frame[1], frame[2], frame[4]);
+    vals[i] = static_cast<uint32_t>(i);
+}
+
+// ---- onesweep radix sort ---------------------------------------------------------------------
+__global__ void k_sort_hist(const uint64_t* __restrict__ keys, int n, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[PASSES][RADIX];
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) (&h[0][0])[k] = 0;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 255], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < PASSES * RADIX; k += blockDim.x) {
+        const unsigned v = (&h[0][0])[k];
+        if (v) atomicAdd(&hist[k], v);
+    }
+}
+
+// Exclusive digit offsets per pass; a pass whose digit is constant over all keys is skipped.
+__global__ void k_sort_offsets(unsigned* __restrict__ hist, int n, SortCtl* ctl) {
+    __shared__ unsigned s[RADIX];
+    const int d = threadIdx.x;
+    for (int p = 0; p < PASSES; ++p) {
+        const unsigned c = hist[p * RADIX + d];
+        s[d] = c;
+        __syncthreads();
+        // Hillis-Steele inclusive scan over 256 entries.
+        for (int o = 1; o < RADIX; o <<= 1) {
+            unsigned t = d >= o ? s[d - o] : 0;
+            __syncthreads();
+            s[d] += t;
+            __syncthreads();
+        }
+        hist[p * RADIX + d] = s[d] - c;
+        const int full = __syncthreads_or(c == static_cast<unsigned>(n));
+        if (d == 0) {
+            ctl->skip[p] = full ? 1u : 0u;
+            ctl->tile_ctr[p] = 0;
+            ctl->done_ctr[p] = 0;
+        }
+        __syncthreads();
+    }
+    if (d == 0) ctl->sel = 0;
+}
+
+__global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA, uint32_t* __restrict__ vA,
+                                                       uint64_t* __restrict__ kB, uint32_t* __restrict__ vB, int n,
+                                                       int pass, const unsigned* __restrict__ offsets,
+                                                       unsigned* __restrict__ lookback, SortCtl* ctl,
+                                                       unsigned* err) {
+    __shared__ unsigned warp_hist[SORT_BS / 32][RADIX];
+    __shared__ unsigned gbase[RADIX];
+    __shared__ unsigned tile_s, sel_s;
+    if (ctl->skip[pass]) return;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        tile_s = atomicAdd(&ctl->tile_ctr[pass], 1u);
+        sel_s = *reinterpret_cast<volatile unsigned*>(&ctl->sel);
+    }
+    for (int k = tid; k < (SORT_BS / 32) * RADIX; k += SORT_BS) (&warp_hist[0][0])[k] = 0;
+    __syncthreads();
+    const unsigned tile = tile_s;
+    const unsigned ntiles = (n + SORT_TILE - 1) / SORT_TILE;
+    const uint64_t* src_k = sel_s ? kB : kA;
+    const uint32_t* src_v = sel_s ? vB : vA;
+    uint64_t* dst_k = sel_s ? kA : kB;
+    uint32_t* dst_v = sel_s ? vA : vB;
+    const int shift = 8 * pass;
+    const int wbase = tile * SORT_TILE + w * (32 * SORT_IPT);
+
+    uint64_t key[SORT_IPT];
+    uint32_t val[SORT_IPT];
+    unsigned rank[SORT_IPT];
+    int dig[SORT_IPT];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < SORT_IPT; ++r) {
+        const int i = wbase + r * 32 + lane;
+        const bool valid = i < n;
+        key[r] = valid ? src_k[i] : 0;
+        val[r] = valid ? src_v[i] : 0;
+        const int d = valid ? static_cast<int>((key[r] >> shift) & 255) : -1 - lane;
+        dig[r] = d;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned before = __popc(peers & lt);
+        unsigned basev = 0;
+        if (valid) basev = warp_hist[w][d];
+        __syncwarp();
+        if (valid && before == 0) warp_hist[w][d] = basev + __popc(peers);
+        __syncwarp();
+        rank[r] = basev + before;
+    }
+    __syncthreads();
+    // Per digit: offsets of each warp inside the tile, and the tile's count.
+    unsigned tile_count;
+    {
+        const int d = tid;
+        unsigned run = 0;
+#pragma unroll
+        for (int u = 0; u < SORT_BS / 32; ++u) {
+            const unsigned c = warp_hist[u][d];
+            warp_hist[u][d] = run;
+            run += c;
+        }
+        tile_count = run;
+        volatile unsigned* lb = lookback + static_cast<size_t>(tile) * RADIX;
+        unsigned prefix = 0;
+        if (tile == 0) {
+            lb[d] = FLAG_INC | tile_count;
+        } else {
+            lb[d] = FLAG_AGG | tile_count;
+            int j = static_cast<int>(tile) - 1;
+            unsigned spins = 0;
+            while (j >= 0) {
+                const unsigned sv = *reinterpret_cast<volatile const unsigned*>(&lookback[static_cast<size_t>(j) * RADIX + d]);
+                if (sv & FLAG_INC) {
+                    prefix += sv & VAL_MASK;
+                    break;
+                }
+                if (sv & FLAG_AGG) {
+                    prefix += sv & VAL_MASK;
+                    --j;
+                    continue;
+                }
+                if (++spins > kSpinCap) {
+                    atomicOr(err, kErrWaitTimeout);
+                    break;
+                }
+            }
+            lb[d] = FLAG_INC | ((prefix + tile_count) & VAL_MASK);
+        }
+        gbase[d] = offsets[pass * RADIX + d] + prefix;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < SORT_IPT; ++r) {
+        const int i = wbase + r * 32 + lane;
+        if (i < n) {
+            const int d = dig[r];
+            const unsigned pos = gbase[d] + warp_hist[w][d] + rank[r];
+            dst_k[pos] = key[r];
+            dst_v[pos] = val[r];
+        }
+    }
+    // The last tile to finish flips the buffer selector (every tile has read it by then).
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&ctl->done_ctr[pass], 1u) == ntiles - 1) ctl->sel ^= 1u;
+    }
+}
+
+// Gathers every body array into the other body set in the order of the permutation in vals;
+// copies the sorted keys; optionally carries a second key array through the permutation.
+__global__ void k_permute(const BodyArrays src, BodyArrays dst, const uint64_t* __restrict__ keys,
+                          const uint32_t* __restrict__ vals, uint64_t* __restrict__ skey,
+                          const uint64_t* __restrict__ key1_in, uint64_t* __restrict__ key1_out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = vals[i];
+    skey[i] = keys[i];
+    if (key1_in) key1_out[i] = key1_in[j];
+    dst.x[i] = src.x[j];
+    dst.y[i] = src.y[j];
+    dst.z[i] = src.z[j];
+    dst.hm[i] = src.hm[j];
+    dst.lo[i] = src.lo[j];
+    dst.vx[i] = src.vx[j];
+    dst.vy[i] = src.vy[j];
+    dst.vz[i] = src.vz[j];
+    dst.m[i] = src.m[j];
+    dst.id[i] = src.id[j];
+    dst.cost[i] = src.cost[j];
+}
+
+// After the passes: if the sorted pairs ended in buffer B, copy them to A (so every sort returns
+// its result in A), and reset the selector.
+__global__ void k_sort_finish(uint64_t* __restrict__ kA, uint32_t* __restrict__ vA, const uint64_t* __restrict__ kB,
+                              const uint32_t* __restrict__ vB, const SortCtl* ctl, int n) {
+    if (ctl->sel == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        kA[i] = kB[i];
+        vA[i] = vB[i];
+    }
+}
+
+// ---- exclusive scan (decoupled look-back) ----------------------------------------------------
+constexpr int SCAN_BS = 256, SCAN_IPT = 8, SCAN_TILE = SCAN_BS * SCAN_IPT;
+constexpr unsigned long long SFLAG_AGG = 1ull << 62, SFLAG_INC = 2ull << 62, SVAL = (1ull << 62) - 1;
+
+__global__ void __launch_bounds__(SCAN_BS) k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int n,
+                                                 unsigned long long* state, unsigned* counter, uint32_t* total,
+                                                 unsigned* err) {
+    __shared__ unsigned tile_s;
+    __shared__ unsigned long long warp_tot[SCAN_BS / 32];
+    __shared__ unsigned long long prefix_s;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) tile_s = atomicAdd(counter, 1u);
+    __syncthreads();
+    const unsigned tile = tile_s;
+    const long long base = static_cast<long long>(tile) * SCAN_TILE + static_cast<long long>(tid) * SCAN_IPT;
+    uint32_t v[SCAN_IPT];
+    unsigned long long tsum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0u;
+        tsum += v[k];
+    }
+    // Warp inclusive scan of thread sums.
+    unsigned long long incl = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long run = 0;
+        for (int u = 0; u < SCAN_BS / 32; ++u) {
+            unsigned long long c = warp_tot[u];
+            warp_tot[u] = run;
+            run += c;
+        }
+        const unsigned long long block_total = run;
+        volatile unsigned long long* st = state;
+        unsigned long long prefix = 0;
+        if (tile == 0) {
+            st[0] = SFLAG_INC | block_total;
+        } else {
+            st[tile] = SFLAG_AGG | block_total;
+            long long j = static_cast<long long>(tile) - 1;
+            unsigned spins = 0;
+            while (j >= 0) {
+                const unsigned long long s = st[j];
+                if (s & SFLAG_INC) { prefix += s & SVAL; break; }
+                if (s & SFLAG_AGG) { prefix += s & SVAL; --j; continue; }
+                if (++spins > kSpinCap) { atomicOr(err, kErrWaitTimeout); break; }
+            }
+            st[tile] = SFLAG_INC | ((prefix + block_total) & SVAL);
+        }
+        prefix_s = prefix;
+        const unsigned ntiles = static_cast<unsigned>((n + SCAN_TILE - 1) / SCAN_TILE);
+        if (tile == ntiles - 1 && total) *total = static_cast<uint32_t>(prefix + block_total);
+    }
+    __syncthreads();
+    unsigned long long run = prefix_s + warp_tot[w] + (incl - tsum);
+#pragma unroll
+    for (int k = 0; k < SCAN_IPT; ++k) {
+        if (base + k < n) out[base + k] = static_cast<uint32_t>(run);
+        run += v[k];
+    }
+}
+
+// ---- key restarts ----------------------------------------------------------------------------
+// A run of identical frame-0 keys longer than LEAF_MAX: appended as (start, end).
+__global__ void k_find_runs(const uint64_t* __restrict__ skey, int n, uint2* runs, unsigned* count, int cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i + LEAF_MAX >= n) return;
+    const uint64_t k = skey[i];
+    if (i > 0 && skey[i - 1] == k) return;
+    if (skey[i + LEAF_MAX] != k) return;
+    int lo = i + LEAF_MAX, hi = n;  // first index with a different key
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (skey[mid] == k) lo = mid + 1;
+        else hi = mid;
+    }
+    const unsigned r = atomicAdd(count, 1u);
+    if (static_cast<int>(r) < cap) runs[r] = make_uint2(static_cast<unsigned>(i), static_cast<unsigned>(lo));
+}
+
+// One block per run: FP64 bounding box (src/cpu_backend.cpp:505-512); cube = (mn, side, scale),
+// side 0 marks coincident bodies (kept as one leaf).
+__global__ void k_run_cube(const BodyArrays b, const uint2* runs, double* cube) {
+    __shared__ double sh[6][BS / 32];
+    const uint2 r = runs[blockIdx.x];
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (unsigned i = r.x + threadIdx.x; i < r.y; i += BS) {
+        double p[3] = {b.x[i], b.y[i], b.z[i]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fmin(v[c], p[c]);
+            v[3 + c] = fmax(v[3 + c], p[c]);
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            double t = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
+        }
+        if (lane == 0) sh[c][w] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double q[6];
+        for (int c = 0; c < 6; ++c) {
+            q[c] = sh[c][0];
+            for (int u = 1; u < BS / 32; ++u) q[c] = c < 3 ? fmin(q[c], sh[c][u]) : fmax(q[c], sh[c][u]);
+        }
+        double side = fmax(fmax(__dsub_rn(q[3], q[0]), __dsub_rn(q[4], q[1])), __dsub_rn(q[5], q[2]));
+        double* o = cube + 5 * blockIdx.x;
+        o[0] = q[0];
+        o[1] = q[1];
+        o[2] = q[2];
+        if (side == 0) {
+            o[3] = 0;
+            o[4] = 0;
+        } else {
+            side = __dmul_rn(side, 1 + 1e-6);
+            o[3] = side;
+            o[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
+        }
+    }
+}
+
+// Restart keys for bodies of non-coincident runs (0 elsewhere); runid = run index or -1.
+__global__ void k_run_keys(const BodyArrays b, const uint2* runs, const double* cube, uint64_t* key1, int* runid) {
+    const uint2 r = runs[blockIdx.x];
+    const double* c = cube + 5 * blockIdx.x;
+    for (unsigned i = r.x + threadIdx.x; i < r.y; i += BS) {
+        runid[i] = static_cast<int>(blockIdx.x);
+        key1[i] = c[3] > 0 ? morton(b.x[i], b.y[i], b.z[i], c[0], c[1], c[2], c[4]) : 0ull;
+    }
+}
+
+__global__ void k_fill_u64(uint64_t* a, uint64_t v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void k_fill_i32(int* a, int v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void k_iota(uint32_t* a, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = static_cast<uint32_t>(i);
+}
+// keys[i] = src[vals[i]]: carries a key array through the permutation in vals.
+__global__ void k_gather_keys(const uint64_t* __restrict__ src, const uint32_t* __restrict__ vals,
+                              uint64_t* __restrict__ keys, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = src[vals[i]];
+}
+
+// ---- leaves ----------------------------------------------------------------------------------
+// Per body: leaf depth and group depth from window common prefixes; cap(i) = 21 inside a
+// coincident frame-0 run, 42 otherwise. bdepth packs (leaf depth, group depth) as bytes.
+__global__ void k_body_depth(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+                             const int* __restrict__ runid, const double* __restrict__ cube, int n, int gmax,
+                             uint16_t* __restrict__ bdepth) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int best = -1;
+    for (int j = max(0, i - LEAF_MAX); j <= i && j + LEAF_MAX < n; ++j) best = max(best, cpl42(k0, k1, j, j + LEAF_MAX));
+    int cap = MAX_DEPTH;
+    if (runid && runid[i] >= 0 && cube[5 * runid[i] + 3] == 0) cap = MAX_LEVEL;
+    if (!k1) cap = MAX_LEVEL;
+    const int ld = min(best + 1, cap);
+    int gbest = -1;
+    for (int j = max(0, i - gmax); j <= i && j + gmax < n; ++j) gbest = max(gbest, cpl42(k0, k1, j, j + gmax));
+    const int gd = min(ld, gbest + 1);
+    bdepth[i] = static_cast<uint16_t>(ld | (gd << 8));
+}
+
+__global__ void k_leaf_flags(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+                             const uint16_t* __restrict__ bdepth, int n, uint32_t* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int d = bdepth[i] & 255;
+    uint32_t f = 1;
+    if (i > 0 && (bdepth[i - 1] & 255) == d && cpl42(k0, k1, i - 1, i) >= d) f = 0;
+    flag[i] = f;
+}
+
+// leaf_first, leaf_depth, leaf_c, and the node count of each leaf (its owned ancestors + itself).
+__global__ void k_leaf_info(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+                            const uint16_t* __restrict__ bdepth, const uint32_t* __restrict__ flag,
+                            const uint32_t* __restrict__ lid, int n, uint32_t* leaf_first, uint8_t* leaf_depth,
+                            int8_t* leaf_c, uint32_t* leaf_nodes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    const uint32_t l = lid[i];
+    const int d = bdepth[i] & 255;
+    const int c = i == 0 ? -1 : cpl42(k0, k1, i - 1, i);
+    leaf_first[l] = static_cast<uint32_t>(i);
+    leaf_depth[l] = static_cast<uint8_t>(d);
+    leaf_c[l] = static_cast<int8_t>(c);
+    leaf_nodes[l] = static_cast<uint32_t>(d - 1 - c + 1);
+}
+
+// ---- nodes -----------------------------------------------------------------------------------
+struct NodeCtx {
+    const uint64_t* k0;
+    const uint64_t* k1;
+    const uint32_t* leaf_first;  // K+1
+    const uint8_t* leaf_depth;
+    const int8_t* leaf_c;
+    const uint32_t* leaf_pre;    // K+1
+    const uint32_t* lid;         // per body
+    const uint16_t* bdepth;
+    int n, K;
+};
+
+// Pre-order index of the node at depth d whose first body is b (b must start that node).
+__device__ __forceinline__ uint32_t node_at(const NodeCtx& c, uint32_t b, int d) {
+    const uint32_t l = c.lid[b];
+    return c.leaf_pre[l] + static_cast<uint32_t>(d - c.leaf_c[l] - 1);
+}
+
+// End of the body range sharing `d` octal digits with body lo.
+__device__ __forceinline__ uint32_t range_end(const NodeCtx& c, uint32_t lo, int d) {
+    uint32_t a = lo + 1, b = static_cast<uint32_t>(c.n);
+    while (a < b) {
+        uint32_t mid = (a + b) >> 1;
+        if (cpl42(c.k0, c.k1, lo, mid) >= d) a = mid + 1;
+        else b = mid;
+    }
+    return a;
+}
+
+// Per pre-order node: (lo, hi) and meta = depth | leaf << 8 | group << 9.
+__global__ void k_nodes_pre(NodeCtx c, uint32_t T, uint2* pn_lohi, uint16_t* pn_meta) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= T) return;
+    // Leaf owning v: last l with leaf_pre[l] <= v.
+    int a = 0, b = c.K;
+    while (b - a > 1) {
+        int mid = (a + b) >> 1;
+        if (c.leaf_pre[mid] <= v) a = mid;
+        else b = mid;
+    }
+    const int l = a;
+    const int d = c.leaf_c[l] + 1 + static_cast<int>(v - c.leaf_pre[l]);
+    const bool leaf = d == c.leaf_depth[l];
+    const uint32_t lo = c.leaf_first[l];
+    const uint32_t hi = leaf ? c.leaf_first[l + 1] : range_end(c, lo, d);
+    const bool group = d == (c.bdepth[lo] >> 8);
+    pn_lohi[v] = make_uint2(lo, hi);
+    pn_meta[v] = static_cast<uint16_t>(d | (leaf ? 256 : 0) | (group ? 512 : 0));
+}
+
+// Children of internal pre-order node v, in order; returns the count.
+template <class F>
+__device__ __forceinline__ int for_children(const NodeCtx& c, const uint2* pn_lohi, uint32_t v, int d, F&& f) {
+    const uint2 r = pn_lohi[v];
+    uint32_t b = r.x;
+    int k = 0;
+    // An octree node has at most 8 children; the cap keeps a malformed range from looping.
+    while (b < r.y && k < 8) {
+        const uint32_t ch = node_at(c, b, d + 1);
+        f(k, ch);
+        const uint32_t nb = pn_lohi[ch].y;
+        if (nb <= b) break;
+        b = nb;
+        ++k;
+    }
+    return k;
+}
+
+__global__ void k_nchild(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta, uint32_t* pn_nchild) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= T) return;
+    const uint16_t meta = pn_meta[v];
+    int k = 0;
+    if (!(meta & 256)) k = for_children(c, pn_lohi, v, meta & 255, [](int, uint32_t) {});
+    pn_nchild[v] = static_cast<uint32_t>(k);
+}
+
+__global__ void k_cpu_index(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta,
+                            const uint32_t* pn_cb, uint32_t* pn_cpu) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= T) return;
+    if (v == 0) pn_cpu[0] = 0;
+    const uint16_t meta = pn_meta[v];
+    if (meta & 256) return;
+    const uint32_t first = 1 + pn_cb[v];
+    for_children(c, pn_lohi, v, meta & 255, [&](int k, uint32_t ch) { pn_cpu[ch] = first + k; });
+}
+
+// Geometric centre (FP64, the reference's iterative halving, src/cpu_backend.cpp:575-582 and
+// 585-592) of the node at depth d containing body b; restart cube at depth 21 for restarted runs.
+__device__ void node_geo(const NodeCtx& c, const double* frame, const int* runid, const double* cube, uint32_t b,
+                         int d, double& gx, double& gy, double& gz, double& half) {
+    half = 0.5 * frame[3];
+    gx = __dadd_rn(frame[0], half);
+    gy = __dadd_rn(frame[1], half);
+    gz = __dadd_rn(frame[2], half);
+    for (int l = 1; l <= d; ++l) {
+        const int o = digit_at(c.k0, c.k1, b, l);
+        const double q = 0.5 * half;
+        gx = __dadd_rn(gx, (o & 4) ? q : -q);
+        gy = __dadd_rn(gy, (o & 2) ? q : -q);
+        gz = __dadd_rn(gz, (o & 1) ? q : -q);
+        half = q;
+        if (l == MAX_LEVEL && runid && runid[b] >= 0) {
+            const double* cb = cube + 5 * runid[b];
+            if (cb[3] > 0) {
+                half = 0.5 * cb[3];
+                gx = __dadd_rn(cb[0], half);
+                gy = __dadd_rn(cb[1], half);
+                gz = __dadd_rn(cb[2], half);
+            }
+        }
+    }
+}
+
+__global__ void k_nodes_out(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta,
+                            const uint32_t* pn_nchild, const uint32_t* pn_cb, const uint32_t* pn_cpu,
+                            const double* frame, const int* runid, const double* cube, uint4* nd_range,
+                            float4* nd_geo, uint32_t* nd_parent, uint32_t* leaf_node, const uint32_t* gidx,
+                            uint32_t* grp_node, int* max_depth, unsigned* err) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= T) return;
+    const uint16_t meta = pn_meta[v];
+    const int d = meta & 255;
+    const bool leaf = meta & 256;
+    const uint2 r = pn_lohi[v];
+    const uint32_t me = pn_cpu[v];
+    const uint32_t nch = pn_nchild[v];
+    const uint32_t first = leaf ? r.x : 1 + pn_cb[v];
+    if (me >= T || (!leaf && first + nch > T) || r.x >= r.y || r.y > static_cast<uint32_t>(c.n)) {
+        atomicOr(err, kErrNodeOverflow);
+        return;
+    }
+    nd_range[me] = make_uint4(r.x, r.y, first, leaf ? 0u : nch);
+    double gx, gy, gz, half;
+    node_geo(c, frame, runid, cube, r.x, d, gx, gy, gz, half);
+    nd_geo[me] = make_float4(static_cast<float>(gx), static_cast<float>(gy), static_cast<float>(gz),
+                             static_cast<float>(half));
+    if (v == 0) nd_parent[0] = 0xffffffffu;
+    if (!leaf)
+        for (uint32_t k = 0; k < nch; ++k) nd_parent[first + k] = me;
+    if (leaf) {
+        const uint32_t l = c.lid[r.x];
+        if (l < static_cast<uint32_t>(c.K)) leaf_node[l] = me;
+        else atomicOr(err, kErrNodeOverflow);
+    }
+    if (meta & 512) {
+        const uint32_t gi = gidx[v];
+        if (gi < T) grp_node[gi] = v;
+        else atomicOr(err, kErrNodeOverflow);
+    }
+    atomicMax(max_depth, d);
+}
+
+// Group boxes from the bodies' float positions (src/cpu_backend.cpp:604-616).
+__global__ void k_groups(const uint32_t* grp_node, const uint2* pn_lohi, uint32_t T, const BodyArrays b,
+                         const unsigned* ngroups, uint2* grp_range, float4* grp_box) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= *ngroups) return;
+    const uint32_t v = grp_node[g];
+    if (v >= T) return;
+    const uint2 r = pn_lohi[v];
+    if (r.x >= r.y) return;
+    float4 p = b.hm[r.x];
+    float mnx = p.x, mny = p.y, mnz = p.z, mxx = mnx, mxy = mny, mxz = mnz;
+    for (uint32_t i = r.x + 1; i < r.y; ++i) {
+        p = b.hm[i];
+        mnx = fminf(mnx, p.x); mny = fminf(mny, p.y); mnz = fminf(mnz, p.z);
+        mxx = fmaxf(mxx, p.x); mxy = fmaxf(mxy, p.y); mxz = fmaxf(mxz, p.z);
+    }
+    grp_range[g] = r;
+    grp_box[2 * g] = make_float4(__fmul_rn(0.5f, __fadd_rn(mnx, mxx)), __fmul_rn(0.5f, __fadd_rn(mny, mxy)),
+                                 __fmul_rn(0.5f, __fadd_rn(mnz, mxz)), 0.f);
+    grp_box[2 * g + 1] = make_float4(__fmul_rn(0.5f, __fsub_rn(mxx, mnx)), __fmul_rn(0.5f, __fsub_rn(mxy, mny)),
+                                     __fmul_rn(0.5f, __fsub_rn(mxz, mnz)), 0.f);
+}
+
+// ---- upsweep ---------------------------------------------------------------------------------
+struct Moments {
+    float4* com;    // (cx, cy, cz, m), the reference's stored floats
+    float4* comlo;  // FP64 com minus its float, as floats
+    float4* q0;     // (qxx, qxy, qxz, qyy)
+    float4* q1;     // (qyz, qzz, rcrit2, 0)
+};
+
+// rcrit2 = (2 half / theta + |com - centre|)^2 capped at FLT_MAX (src/cpu_backend.cpp:595-600).
+__device__ __forceinline__ float rcrit2_of(float cx, float cy, float cz, float4 g, float inv_theta) {
+    const float dx = __fsub_rn(cx, g.x), dy = __fsub_rn(cy, g.y), dz = __fsub_rn(cz, g.z);
+    const float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const double r = __dadd_rn(__dmul_rn(static_cast<double>(__fmul_rn(2.f, g.w)), static_cast<double>(inv_theta)),
+                               __dsqrt_rn(static_cast<double>(s)));
+    const double r2 = __dmul_rn(r, r);
+    return static_cast<float>(r2 < static_cast<double>(FLT_MAX) ? r2 : static_cast<double>(FLT_MAX));
+}
+
+__device__ void store_moments(Moments mo, uint32_t node, double M, double cx, double cy, double cz, double qxx,
+                              double qxy, double qxz, double qyy, double qyz, double qzz, float4 g, float inv_theta) {
+    const float fx = static_cast<float>(cx), fy = static_cast<float>(cy), fz = static_cast<float>(cz);
+    mo.com[node] = make_float4(fx, fy, fz, static_cast<float>(M));
+    mo.comlo[node] = make_float4(static_cast<float>(__dsub_rn(cx, fx)), static_cast<float>(__dsub_rn(cy, fy)),
+                                 static_cast<float>(__dsub_rn(cz, fz)), 0.f);
+    mo.q0[node] = make_float4(static_cast<float>(qxx), static_cast<float>(qxy), static_cast<float>(qxz),
+                              static_cast<float>(qyy));
+    mo.q1[node] = make_float4(static_cast<float>(qyz), static_cast<float>(qzz), rcrit2_of(fx, fy, fz, g, inv_theta), 0.f);
+}
+
+#define DADD __dadd_rn
+#define DMUL __dmul_rn
+#define DSUB __dsub_rn
+
+__global__ void k_upsweep(const uint32_t* __restrict__ leaf_node, uint32_t K, uint32_t T,
+                          const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo,
+                          const uint32_t* __restrict__ nd_parent, unsigned* arrive, const BodyArrays b, Moments mo,
+                          float inv_theta, unsigned* err) {
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= K) return;
+    uint32_t node = leaf_node[l];
+    if (node >= T) {
+        atomicOr(err, kErrNodeOverflow);
+        return;
+    }
+    {
+        // Leaf moments about the leaf's centre of mass (src/cpu_backend.cpp:619-640).
+        const uint4 r = nd_range[node];
+        const float4 g = nd_geo[node];
+        double M = 0, sx = 0, sy = 0, sz = 0;
+        for (uint32_t i = r.x; i < r.y; ++i) {
+            const double m = b.m[i];
+            M = DADD(M, m);
+            sx = DADD(sx, DMUL(m, b.x[i]));
+            sy = DADD(sy, DMUL(m, b.y[i]));
+            sz = DADD(sz, DMUL(m, b.z[i]));
+        }
+        const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
+                     cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
+        double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
+        for (uint32_t i = r.x; i < r.y; ++i) {
+            const double m = b.m[i], dx = DSUB(b.x[i], cx), dy = DSUB(b.y[i], cy), dz = DSUB(b.z[i], cz);
+            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+            qxx = DADD(qxx, DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
+            qyy = DADD(qyy, DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
+            qzz = DADD(qzz, DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
+            qxy = DADD(qxy, DMUL(DMUL(DMUL(m, 3.0), dx), dy));
+            qxz = DADD(qxz, DMUL(DMUL(DMUL(m, 3.0), dx), dz));
+            qyz = DADD(qyz, DMUL(DMUL(DMUL(m, 3.0), dy), dz));
+        }
+        store_moments(mo, node, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+    }
+    // Climb: the last child to arrive at a parent combines all of its children in index order.
+    // A path is at most 2*21+1 nodes long; the cap and the range checks stop a malformed tree.
+    for (int steps = 0; node != 0; ++steps) {
+        const uint32_t p = nd_parent[node];
+        if (p >= T || steps > 4 * MAX_DEPTH) {
+            atomicOr(err, kErrNodeOverflow);
+            return;
+        }
+        const uint4 r = nd_range[p];
+        if (r.w == 0 || r.z + r.w > T) {
+            atomicOr(err, kErrNodeOverflow);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1u) != r.w - 1) return;
+        __threadfence();
+        const float4 g = nd_geo[p];
+        double M = 0, sx = 0, sy = 0, sz = 0;
+        for (uint32_t c = r.z; c < r.z + r.w; ++c) {
+            const float4 cm = __ldcg(&mo.com[c]);
+            const double m = cm.w;
+            M = DADD(M, m);
+            sx = DADD(sx, DMUL(m, static_cast<double>(cm.x)));
+            sy = DADD(sy, DMUL(m, static_cast<double>(cm.y)));
+            sz = DADD(sz, DMUL(m, static_cast<double>(cm.z)));
+        }
+        const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
+                     cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
+        double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
+        for (uint32_t c = r.z; c < r.z + r.w; ++c) {
+            const float4 cm = __ldcg(&mo.com[c]);
+            const float4 a = __ldcg(&mo.q0[c]);
+            const float4 e = __ldcg(&mo.q1[c]);
+            const double m = cm.w, dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
+                         dz = DSUB(static_cast<double>(cm.z), cz);
+            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+            qxx = DADD(qxx, DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2))));
+            qyy = DADD(qyy, DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2))));
+            qzz = DADD(qzz, DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2))));
+            qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(DMUL(m, 3.0), dx), dy)));
+            qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(DMUL(m, 3.0), dx), dz)));
+            qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(DMUL(m, 3.0), dy), dz)));
+        }
+        store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+        node = p;
+    }
+}
+
+#undef DADD
+#undef DMUL
+#undef DSUB
+
+
+__global__ void k_lid(uint32_t* lid, const uint32_t* flag, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) lid[i] = lid[i] + flag[i] - 1;
+}
+
+__global__ void k_leaf_tail(uint32_t* leaf_first, const unsigned* K, int n) { leaf_first[*K] = static_cast<uint32_t>(n); }
+
+__global__ void k_gflag(const uint16_t* pn_meta, uint32_t T, uint32_t* gflag) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < T) gflag[v] = (pn_meta[v] >> 9) & 1u;
+}
+
+__global__ void k_probe() {}
+
+// ---- host helpers ----------------------------------------------------------------------------
+void scan_u32(Engine& e, TreeState& t, const uint32_t* in, uint32_t* out, int n, uint32_t* total) {
+    if (n <= 0) return;
+    const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    t.scan_state.reserve(static_cast<size_t>(tiles) * 8);
+    t.scan_ctr.reserve(256);
+    LG_CK(cudaMemsetAsync(t.scan_state.as<char>(), 0, static_cast<size_t>(tiles) * 8, e.stream));
+    LG_CK(cudaMemsetAsync(t.scan_ctr.as<char>(), 0, 4, e.stream));
+    k_scan<<<tiles, SCAN_BS, 0, e.stream>>>(in, out, n, t.scan_state.as<unsigned long long>(), t.scan_ctr.as<unsigned>(),
+                                           total, e.err_word());
+    LG_LAUNCHED();
+    ++e.launches;
+}
+
+// Sorts (keys, vals) held in (keysA, valsA); result in the buffer ctl->sel selects.
+void sort_pairs(Engine& e, TreeState& t, int n) {
+    cudaStream_t s = e.stream;
+    const int tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    t.hist.reserve(PASSES * RADIX * 4);
+    t.lookback.reserve(static_cast<size_t>(PASSES) * tiles * RADIX * 4);
+    t.ctl.reserve(sizeof(SortCtl));
+    LG_CK(cudaMemsetAsync(t.hist.as<char>(), 0, PASSES * RADIX * 4, s));
+    LG_CK(cudaMemsetAsync(t.lookback.as<char>(), 0, static_cast<size_t>(PASSES) * tiles * RADIX * 4, s));
+    const int hb = std::min(e.sms * 4, std::max(1, grid_for(n, 1024)));
+    k_sort_hist<<<hb, 256, 0, s>>>(t.keysA.as<uint64_t>(), n, t.hist.as<unsigned>());
+    LG_LAUNCHED();
+    k_sort_offsets<<<1, RADIX, 0, s>>>(t.hist.as<unsigned>(), n, t.ctl.as<SortCtl>());
+    LG_LAUNCHED();
+    for (int p = 0; p < PASSES; ++p) {
+        k_sort_pass<<<tiles, SORT_BS, 0, s>>>(t.keysA.as<uint64_t>(), t.valsA.as<uint32_t>(), t.keysB.as<uint64_t>(),
+                                              t.valsB.as<uint32_t>(), n, p, t.hist.as<unsigned>(),
+                                              t.lookback.as<unsigned>() + static_cast<size_t>(p) * tiles * RADIX,
+                                              t.ctl.as<SortCtl>(), e.err_word());
+        LG_LAUNCHED();
+    }
+    k_sort_finish<<<std::max(1, std::min(4 * e.sms, grid_for(n, BS))), BS, 0, s>>>(
+        t.keysA.as<uint64_t>(), t.valsA.as<uint32_t>(), t.keysB.as<uint64_t>(), t.valsB.as<uint32_t>(),
+        t.ctl.as<SortCtl>(), n);
+    LG_LAUNCHED();
+    e.launches += 3 + PASSES;
+}
+
+void reserve_sort(TreeState& t, int n) {
+    const size_t cnt = static_cast<size_t>(n) + 1;
+    t.keysA.reserve(cnt * 8); t.keysB.reserve(cnt * 8);
+    t.valsA.reserve(cnt * 4); t.valsB.reserve(cnt * 4);
+    t.skey.reserve(cnt * 8);
+}
+
+}  // namespace
+
+std::unique_ptr<TreeState, void (*)(TreeState*)> make_tree_state() {
+    return std::unique_ptr<TreeState, void (*)(TreeState*)>(new TreeState, destroy_tree);
+}
+
+const void* probe_kernel() { return reinterpret_cast<const void*>(k_probe); }
+
+void tree_sort(Engine& e) {
+    TreeState& t = *e.tree;
+    const int n = e.n;
+    cudaStream_t s = e.stream;
+    if (n >= (1 << 30)) fail(kRuntime, "cuda tree: n >= 2^30 exceeds the sort's look-back counters");
+    reserve_sort(t, n);
+    t.frame.reserve(64);
+    t.counts.reserve(64);
+    t.restarted = false;
+    t.nruns = 0;
+    const int fb = std::min(1024, grid_for(n, BS));
+    e.diag_partial.reserve(static_cast<size_t>(fb) * 12 * 8);
+    k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<double>(), e.ticket(), t.frame.as<double>());
+    LG_LAUNCHED();
+    k_keys<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), n, t.frame.as<double>(), t.keysA.as<uint64_t>(),
+                                          t.valsA.as<uint32_t>());
+    LG_LAUNCHED();
+    e.launches += 2;
+    sort_pairs(e, t, n);
+    int other = e.cur ^ 1;
+    k_permute<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
+                                             t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), nullptr, nullptr, n);
+    LG_LAUNCHED();
+    ++e.launches;
+    e.cur = other;
+
+    // Key restarts (src/cpu_backend.cpp:541-544): runs of identical keys longer than a leaf.
+    unsigned* counts = t.counts.as<unsigned>();
+    LG_CK(cudaMemsetAsync(counts, 0, 64, s));
+    const int run_cap = std::max(1, n / (LEAF_MAX + 1) + 1);
+    t.runs.reserve(static_cast<size_t>(run_cap) * 8);
+    k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), n, t.runs.as<uint2>(), counts, run_cap);
+    LG_LAUNCHED();
+    ++e.launches;
+    LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 4, cudaMemcpyDeviceToHost, s));
+    LG_CK(cudaStreamSynchronize(s));
+    const unsigned R = e.pinned_small[0];
+    if (R == 0) return;
+    t.nruns = R;
+    t.restarted = true;
+    BodyArrays b = e.bodies(e.cur);
+    t.runcube.reserve(static_cast<size_t>(R) * 5 * 8);
+    t.runid.reserve(static_cast<size_t>(n) * 4);
+    t.skey1.reserve(static_cast<size_t>(n) * 8 + 8);
+    t.key1tmp.reserve(static_cast<size_t>(n) * 8 + 8);
+    uint64_t* key1 = t.key1tmp.as<uint64_t>();
+    k_fill_i32<<<grid_for(n, BS), BS, 0, s>>>(t.runid.as<int>(), -1, n);
+    LG_LAUNCHED();
+    k_fill_u64<<<grid_for(n, BS), BS, 0, s>>>(key1, 0ull, n);
+    LG_LAUNCHED();
+    k_run_cube<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.runcube.as<double>());
+    LG_LAUNCHED();
+    k_run_keys<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.runcube.as<double>(), key1, t.runid.as<int>());
+    LG_LAUNCHED();
+    e.launches += 4;
+    // Stable sort by (key, restart key): LSD on the restart key, then on the key. Runs are ranges of
+    // equal keys, so every body stays inside its run and runid (by position) stays valid.
+    LG_CK(cudaMemcpyAsync(t.keysA.as<uint64_t>(), key1, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToDevice, s));
+    k_iota<<<grid_for(n, BS), BS, 0, s>>>(t.valsA.as<uint32_t>(), n);
+    LG_LAUNCHED();
+    sort_pairs(e, t, n);
+    k_gather_keys<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), t.valsA.as<uint32_t>(), t.keysA.as<uint64_t>(), n);
+    LG_LAUNCHED();
+    e.launches += 2;
+    sort_pairs(e, t, n);
+    other = e.cur ^ 1;
+    k_permute<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
+                                             t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), key1,
+                                             t.skey1.as<uint64_t>(), n);
+    LG_LAUNCHED();
+    ++e.launches;
+    e.cur = other;
+}
+
+void tree_build(Engine& e, double theta) {
+    TreeState& t = *e.tree;
+    const int n = e.n;
+    cudaStream_t s = e.stream;
+    t.group_max = e.group_max;
+    const uint64_t* k0 = t.skey.as<uint64_t>();
+    const uint64_t* k1 = t.restarted ? t.skey1.as<uint64_t>() : nullptr;
+    const int* runid = t.restarted ? t.runid.as<int>() : nullptr;
+    const double* cube = t.restarted ? t.runcube.as<double>() : nullptr;
+    unsigned* counts = t.counts.as<unsigned>();
+    const size_t n1 = static_cast<size_t>(n) + 1;
+    t.bdepth.reserve(n1 * 2);
+    t.flag.reserve(n1 * 4);
+    t.leafid.reserve(n1 * 4);
+    t.leaf_first.reserve(n1 * 4);
+    t.leaf_depth.reserve(n1);
+    t.leaf_c.reserve(n1);
+    t.leaf_cnt.reserve(n1 * 4);
+    t.leaf_pre.reserve(n1 * 4);
+    t.leaf_node.reserve(n1 * 4);
+    const int gb = grid_for(n, BS);
+    k_body_depth<<<gb, BS, 0, s>>>(k0, k1, runid, cube, n, t.group_max, t.bdepth.as<uint16_t>());
+    LG_LAUNCHED();
+    k_leaf_flags<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
+    LG_LAUNCHED();
+    e.launches += 2;
+    scan_u32(e, t, t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n, counts + 1);
+    LG_CK(cudaMemsetAsync(t.leaf_cnt.as<char>(), 0, n1 * 4, s));
+    k_leaf_info<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
+                                  t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
+                                  t.leaf_cnt.as<uint32_t>());
+    LG_LAUNCHED();
+    k_lid<<<gb, BS, 0, s>>>(t.leafid.as<uint32_t>(), t.flag.as<uint32_t>(), n);
+    LG_LAUNCHED();
+    k_leaf_tail<<<1, 1, 0, s>>>(t.leaf_first.as<uint32_t>(), counts + 1, n);
+    LG_LAUNCHED();
+    e.launches += 3;
+    scan_u32(e, t, t.leaf_cnt.as<uint32_t>(), t.leaf_pre.as<uint32_t>(), n + 1, counts + 2);
+    LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 16, cudaMemcpyDeviceToHost, s));
+    LG_CK(cudaStreamSynchronize(s));
+    t.K = e.pinned_small[1];
+    t.T = e.pinned_small[2];
+    const size_t K = t.K, T = t.T;
+    if (K < 1 || K > static_cast<size_t>(n) || T < K)
+        fail(kRuntime, "cuda tree build: bad leaf/node count " + std::to_string(K) + "/" + std::to_string(T));
+    t.pn_lohi.reserve(T * 8);
+    t.pn_meta.reserve(T * 2);
+    t.pn_nchild.reserve(T * 4);
+    t.pn_cb.reserve(T * 4);
+    t.pn_cpu.reserve(T * 4);
+    t.gflag.reserve(T * 4);
+    t.gidx.reserve(T * 4);
+    t.grp_node.reserve(T * 4);
+    t.grp_range.reserve(T * 8);
+    t.grp_box.reserve(T * 32);
+    for (DevBuf* d : {&t.nd_range, &t.nd_com, &t.nd_comlo, &t.nd_q0, &t.nd_q1, &t.nd_geo}) d->reserve(T * 16);
+    t.nd_parent.reserve(T * 4);
+    t.nd_arrive.reserve(T * 4);
+    NodeCtx c{k0, k1, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
+              t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, static_cast<int>(K)};
+    const int tb = grid_for(static_cast<long long>(T), BS);
+    // Index arrays start out of range (0xff..): a slot the construction fails to fill is caught by
+    // the range checks below instead of being followed.
+    LG_CK(cudaMemsetAsync(t.pn_cpu.as<char>(), 0xff, T * 4, s));
+    LG_CK(cudaMemsetAsync(t.grp_node.as<char>(), 0xff, T * 4, s));
+    LG_CK(cudaMemsetAsync(t.leaf_node.as<char>(), 0xff, K * 4, s));
+    LG_CK(cudaMemsetAsync(t.nd_parent.as<char>(), 0xff, T * 4, s));
+    LG_CK(cudaMemsetAsync(t.nd_range.as<char>(), 0, T * 16, s));
+    LG_CK(cudaMemsetAsync(t.grp_range.as<char>(), 0, T * 8, s));
+    k_nodes_pre<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>());
+    LG_LAUNCHED();
+    k_nchild<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
+                               t.pn_nchild.as<uint32_t>());
+    LG_LAUNCHED();
+    e.launches += 2;
+    scan_u32(e, t, t.pn_nchild.as<uint32_t>(), t.pn_cb.as<uint32_t>(), static_cast<int>(T), nullptr);
+    k_gflag<<<tb, BS, 0, s>>>(t.pn_meta.as<uint16_t>(), static_cast<uint32_t>(T), t.gflag.as<uint32_t>());
+    LG_LAUNCHED();
+    ++e.launches;
+    scan_u32(e, t, t.gflag.as<uint32_t>(), t.gidx.as<uint32_t>(), static_cast<int>(T), counts + 3);
+    k_cpu_index<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
+                                  t.pn_cb.as<uint32_t>(), t.pn_cpu.as<uint32_t>());
+    LG_LAUNCHED();
+    k_nodes_out<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
+                                  t.pn_nchild.as<uint32_t>(), t.pn_cb.as<uint32_t>(), t.pn_cpu.as<uint32_t>(),
+                                  t.frame.as<double>(), runid, cube, t.nd_range.as<uint4>(), t.nd_geo.as<float4>(),
+                                  t.nd_parent.as<uint32_t>(), t.leaf_node.as<uint32_t>(), t.gidx.as<uint32_t>(),
+                                  t.grp_node.as<uint32_t>(), reinterpret_cast<int*>(counts + 4), e.err_word());
+    LG_LAUNCHED();
+    k_groups<<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_lohi.as<uint2>(), static_cast<uint32_t>(T),
+                               e.bodies(e.cur), counts + 3,
+                               t.grp_range.as<uint2>(), t.grp_box.as<float4>());
+    LG_LAUNCHED();
+    LG_CK(cudaMemsetAsync(t.nd_arrive.as<char>(), 0, T * 4, s));
+    const float inv_theta = theta > 0 ? static_cast<float>(1.0 / theta) : FLT_MAX;
+    Moments mo{t.nd_com.as<float4>(), t.nd_comlo.as<float4>(), t.nd_q0.as<float4>(), t.nd_q1.as<float4>()};
+    k_upsweep<<<grid_for(static_cast<long long>(K), 128), 128, 0, s>>>(
+        t.leaf_node.as<uint32_t>(), static_cast<uint32_t>(K), static_cast<uint32_t>(T), t.nd_range.as<uint4>(),
+        t.nd_geo.as<float4>(), t.nd_parent.as<uint32_t>(), t.nd_arrive.as<unsigned>(), e.bodies(e.cur), mo,
+        inv_theta, e.err_word());
+    LG_LAUNCHED();
+    e.launches += 4;
+}
+
+TreeView tree_view(Engine& e) {
+    TreeState& t = *e.tree;
+    TreeView v;
+    v.nd_range = t.nd_range.as<uint4>();
+    v.nd_com = t.nd_com.as<float4>();
+    v.nd_comlo = t.nd_comlo.as<float4>();
+    v.nd_q0 = t.nd_q0.as<float4>();
+    v.nd_q1 = t.nd_q1.as<float4>();
+    v.grp_range = t.grp_range.as<uint2>();
+    v.grp_box = t.grp_box.as<float4>();
+    v.ngroups = t.counts.as<unsigned>() + 3;
+    v.T = t.T;
+    return v;
+}
+
+void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth) {
+    TreeState& t = *e.tree;
+    if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    LG_CK(cudaMemcpyAsync(e.pinned_small, t.counts.as<unsigned>(), 32, cudaMemcpyDeviceToHost, e.stream));
+    LG_CK(cudaStreamSynchronize(e.stream));
+    if (nodes) *nodes = e.pinned_small[2];
+    if (leaves) *leaves = e.pinned_small[1];
+    if (groups) *groups = e.pinned_small[3];
+    if (max_depth) *max_depth = static_cast<int>(e.pinned_small[4]);
+}
+
+// The reference's key array after a build (src/cpu_backend.cpp:884-906 key_): frame-0 keys, with the
+// restart keys in place inside re-keyed runs (rekey overwrites key_ there; coincident runs keep
+// their frame-0 keys).
+void tree_keys(Engine& e, uint64_t* keys, size_t n) {
+    TreeState& t = *e.tree;
+    if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    if (n < static_cast<size_t>(e.n)) fail(kArg, "tree_keys: output holds fewer than n keys");
+    const size_t N = static_cast<size_t>(e.n);
+    LG_CK(cudaMemcpyAsync(keys, t.skey.as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));
+    if (t.restarted) {
+        std::vector<uint64_t> k1(N);
+        std::vector<int> rid(N);
+        std::vector<double> cube(t.nruns * 5);
+        LG_CK(cudaMemcpyAsync(k1.data(), t.skey1.as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaMemcpyAsync(rid.data(), t.runid.as<int>(), N * 4, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaMemcpyAsync(cube.data(), t.runcube.as<double>(), cube.size() * 8, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaStreamSynchronize(e.stream));
+        for (size_t i = 0; i < N; ++i)
+            if (rid[i] >= 0 && cube[5 * static_cast<size_t>(rid[i]) + 3] > 0) keys[i] = k1[i];
+    }
+    LG_CK(cudaStreamSynchronize(e.stream));
+}
+
+void tree_nodes(Engine& e, uint32_t* range4, float* moments11, float* geo4, size_t nodes) {
+    TreeState& t = *e.tree;
+    if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    size_t T = 0;
+    tree_counts(e, &T, nullptr, nullptr, nullptr);
+    if (nodes < T) fail(kArg, "tree_nodes: output holds fewer than the node count");
+    if (range4) LG_CK(cudaMemcpyAsync(range4, t.nd_range.as<uint4>(), T * 16, cudaMemcpyDeviceToHost, e.stream));
+    if (geo4) LG_CK(cudaMemcpyAsync(geo4, t.nd_geo.as<float4>(), T * 16, cudaMemcpyDeviceToHost, e.stream));
+    if (moments11) {
+        std::vector<float4> com(T), q0(T), q1(T);
+        LG_CK(cudaMemcpyAsync(com.data(), t.nd_com.as<float4>(), T * 16, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaMemcpyAsync(q0.data(), t.nd_q0.as<float4>(), T * 16, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaMemcpyAsync(q1.data(), t.nd_q1.as<float4>(), T * 16, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaStreamSynchronize(e.stream));
+        for (size_t k = 0; k < T; ++k) {
+            float* o = moments11 + 11 * k;
+            o[0] = com[k].x; o[1] = com[k].y; o[2] = com[k].z; o[3] = com[k].w;
+            o[4] = q0[k].x; o[5] = q0[k].y; o[6] = q0[k].z; o[7] = q0[k].w;
+            o[8] = q1[k].x; o[9] = q1[k].y; o[10] = q1[k].z;
+        }
+    }
+    LG_CK(cudaStreamSynchronize(e.stream));
+}
+
+void tree_groups(Engine& e, float* box6, uint32_t* lohi, size_t groups) {
+    TreeState& t = *e.tree;
+    if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    size_t G = 0;
+    tree_counts(e, nullptr, nullptr, &G, nullptr);
+    if (groups < G) fail(kArg, "tree_groups: output holds fewer than the group count");
+    if (lohi) LG_CK(cudaMemcpyAsync(lohi, t.grp_range.as<uint2>(), G * 8, cudaMemcpyDeviceToHost, e.stream));
+    if (box6) {
+        std::vector<float4> box(2 * G);
+        LG_CK(cudaMemcpyAsync(box.data(), t.grp_box.as<float4>(), G * 32, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaStreamSynchronize(e.stream));
+        for (size_t g = 0; g < G; ++g) {
+            box6[6 * g] = box[2 * g].x; box6[6 * g + 1] = box[2 * g].y; box6[6 * g + 2] = box[2 * g].z;
+            box6[6 * g + 3] = box[2 * g + 1].x; box6[6 * g + 4] = box[2 * g + 1].y; box6[6 * g + 5] = box[2 * g + 1].z;
+        }
+    }
+    LG_CK(cudaStreamSynchronize(e.stream));
+}
+
+lg_memory_estimate memory_need(uint64_t n, int method) {
+    lg_memory_estimate r{};
+    // Two body sets (80 B), accelerations (16 B), staging (12 B), plus fixed buffers.
+    r.device = 192 * n + (uint64_t(64) << 20);
+    if (method == LG_TREE) r.device += 112 * n;  // keys, sort buffers, per-body tree data, ~0.2 n nodes
+    r.host = 0;
+    return r;
+}
+
+size_t tree_held_bytes(const Engine& e) {
+    const TreeState& t = *e.tree;
+    size_t h = 0;
+    for (const DevBuf* d : {&t.keysA, &t.keysB, &t.valsA, &t.valsB, &t.hist, &t.lookback, &t.ctl, &t.skey, &t.skey1, &t.key1tmp,
+                            &t.runid, &t.bdepth, &t.flag, &t.leafid, &t.frame, &t.runs, &t.runcube, &t.counts,
+                            &t.leaf_first, &t.leaf_depth, &t.leaf_c, &t.leaf_pre, &t.leaf_node, &t.pn_lohi,
+                            &t.pn_meta, &t.pn_nchild, &t.pn_cb, &t.pn_cpu, &t.nd_range, &t.nd_com, &t.nd_comlo,
+                            &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.nd_arrive, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt,
+                            &t.grp_range, &t.grp_box, &t.scan_state, &t.scan_ctr})
+        h += d->capacity();
+    return h;
+}
+
+}  // namespace lg

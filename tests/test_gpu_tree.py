@@ -1,0 +1,278 @@
+"""Barnes-Hut tree on the GPU, through the C ABI: bit-exact keys, permutation and topology against
+the reference CPU backend's golden vectors and the live CPU oracle; force accuracy against the
+reference's tree and the FP64 direct sum; the interface semantics of tests/test_cuda_backend.cpp
+and tests/test_cuda_let.cpp:164-183.
+
+Stated tolerances: tree accelerations vs the reference's own tree at the same theta: relative rms
+<= 1e-5 and per-body median relative error <= 1e-5 (same interaction lists; FP32 summation order
+and rsqrt differ). Tree vs FP64 direct at theta 0.6: relative rms <= 1e-3."""
+import os
+
+import numpy as np
+import pytest
+
+import lettuce_simulate_physics_gb300 as L
+from golden_io import Golden, by_id as g_by_id, names
+from gpu_util import accel, by_id, params, per_body_rel, rel_rms, zero_v
+from lettuce_simulate_physics_gb300 import scenarios as S
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+THETA = {"t06": 0.6, "t03": 0.3, "t00": 0.0}
+
+
+@pytest.fixture(scope="module")
+def be():
+    from lettuce_simulate_physics_gb300 import build as B
+    B.build()
+    be, why = L.make_cuda_backend(0)
+    if be is None:
+        pytest.fail(f"no usable device: {why}")
+    yield be
+    be.close()
+
+
+def with_env(env):
+    old = {k: os.environ.get(k) for k in env}
+    try:
+        for k, v in env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        return L.CudaBackend(0)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("name", names("tree_"))
+def test_tree_bit_exact_vs_reference_golden(be, name):
+    g = Golden(name)
+    b = g.inputs()
+    n = len(b)
+    for c in g.cases():
+        ref = g.case(c)
+        pot = bool(ref["has_pe"])
+        be.upload(zero_v(b))
+        p = params(1, g.param("eps"), THETA[c], g.param("G"))
+        be.compute_forces(p, pot)
+        assert np.array_equal(be.tree_keys(), ref["keys"]), "Morton keys"
+        assert np.array_equal(be.download().id, ref["order_id"]), "sort permutation"
+        rng, mom, geo = be.tree_nodes()
+        rn = ref["nodes"]
+        assert len(rng) == len(rn), "node count"
+        for k, f in enumerate(("lo", "hi", "first", "nchild")):
+            assert np.array_equal(rng[:, k], rn[f]), f
+        gg = ref["geo"]
+        for k, f in enumerate(("gx", "gy", "gz", "half")):
+            assert np.array_equal(geo[:, k], gg[f]), f
+        for k, f in enumerate(("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz")):
+            assert np.array_equal(mom[:, k], rn[f]), f
+        np.testing.assert_allclose(mom[:, 10], rn["rcrit2"], rtol=2.5e-7, atol=0)
+        box, lohi = be.tree_groups()
+        rg = ref["groups"]
+        assert np.array_equal(lohi[:, 0], rg["lo"]) and np.array_equal(lohi[:, 1], rg["hi"])
+        for k, f in enumerate(("bx", "by", "bz", "hx", "hy", "hz")):
+            assert np.array_equal(box[:, k], rg[f]), f
+        cnt = be.tree_counts()
+        assert cnt["max_depth"] == int(ref["max_depth"])
+        assert cnt["leaves"] == len(ref["leaves"])
+        t = be.times()
+        # The reference counts each body's own list entry; this engine does not.
+        assert t.interactions == int(ref["interactions"]) - n
+        ok, cost = be.body_costs()
+        assert ok and np.array_equal(cost, ref["costs"] - 1)
+        a = be.accel()
+        ra = ref["acc"]
+        assert rel_rms(a[:3], ra[:3]) <= 1e-5
+        assert np.median(per_body_rel(a[:3], ra[:3])) <= 1e-5
+        if pot:
+            np.testing.assert_allclose(a[3], ra[3], rtol=1e-4, atol=1e-6 * np.abs(ra[3]).max())
+
+
+def test_tree_bit_exact_vs_live_oracle_disk(be):
+    b = S.disk(200_000, 3)
+    p = params(1, 0.005, 0.6)
+    be.upload(zero_v(b))
+    be.compute_forces(p, False)
+    port = O.OracleBackend("port", 0)
+    port.upload(zero_v(b))
+    port.compute_forces(O.TREE, 1.0, 0.005, 0.6, False)
+    assert np.array_equal(be.tree_keys(), port.keys())
+    assert np.array_equal(be.download().id, port.download().id)
+    rng, mom, _ = be.tree_nodes()
+    pn = port.nodes()
+    assert np.array_equal(rng, np.stack([pn["lo"], pn["hi"], pn["first"], pn["nchild"]], 1))
+    assert np.array_equal(mom[:, 3], pn["m"]) and np.array_equal(mom[:, 0], pn["cx"])
+    assert be.times().interactions == port.times()["interactions"] - len(b)
+    assert rel_rms(be.accel()[:3], port.accel()[:3]) <= 1e-5
+
+
+def test_coincident_bodies_theta0_exact_and_theta06(be):
+    b = S.cube(300, 7)
+    b.x[:150] = 0.25
+    b.y[:150] = -0.5
+    b.z[:150] = 0.125
+    k = np.arange(40, dtype=np.float32)
+    b.x[150:190] = np.float32(-0.3) + np.float32(1e-7) * k
+    b.y[150:190] = 0.1
+    b.z[150:190] = 0.2
+    exact = O.direct_fp64(b, 1.0, 0.05)
+    ref_a = by_id(b.id, exact[:3])
+    ref_pe = 0.5 * float((b.m.astype(np.float64) * exact[3]).sum())
+    for bk in (be, with_env({"LETTUCE_CUDA_GROUP": "32"}), with_env({"LETTUCE_CUDA_WALK": "body"})):
+        g0 = accel(bk, b, params(1, 0.05, 0.0), True)
+        assert np.isfinite(g0.a).all()
+        assert rel_rms(g0.a, ref_a) <= 1e-5
+        assert g0.times.interactions == 300 * 299
+        g1 = accel(bk, b, params(1, 0.05, 0.6), True)
+        assert rel_rms(g1.a, ref_a) <= 1e-2
+        assert abs(g1.diag.pe / ref_pe - 1) <= 2e-4
+
+
+def test_tree_vs_direct_20k_theta06(be):
+    b = S.plummer(20000, 2, cut=20)
+    d = accel(be, b, params(0, 0.01), True)
+    t = accel(be, b, params(1, 0.01, 0.6), True)
+    e = rel_rms(t.a, d.a)
+    print(f"rel rms {e:.3g}, {t.times.interactions / 20000:.1f} int/body, force {t.times.force_ms:.3f} ms "
+          f"(sort {t.times.sort_ms:.3f} build {t.times.build_ms:.3f} walk {t.times.walk_ms:.3f})")
+    assert np.isfinite(t.a).all()
+    assert e <= 1e-3
+    assert abs(t.diag.pe / d.diag.pe - 1) <= 1e-3
+    assert 0 < t.times.interactions < 20000 * 19999
+
+
+def test_smaller_groups_give_fewer_interactions_same_accuracy(be):
+    b = S.plummer(20000, 8, cut=20)
+    d = accel(be, b, params(0, 0.01), True)
+    g32 = with_env({"LETTUCE_CUDA_GROUP": "32"})
+    for theta in (0.3, 0.6, 0.9):
+        p = params(1, 0.01, theta)
+        t128 = accel(be, b, p, True)
+        t32 = accel(g32, b, p, True)
+        e128, e32 = rel_rms(t128.a, d.a), rel_rms(t32.a, d.a)
+        assert t128.times.interactions >= t32.times.interactions
+        assert e128 <= 1.02 * e32 + 1e-6
+        for bk in (be, g32):
+            ok, cost = bk.body_costs()
+            assert ok and float(cost.astype(np.float64).sum()) == bk.times().interactions
+
+
+def test_download_after_tree_steps_returns_every_id_once(be):
+    b = S.plummer(5000, 5, cut=20)
+    p = params(1, 0.01, 0.6)
+    be.upload(b)
+    be.compute_forces(p, False)
+    for _ in range(5):
+        be.kick(0.005)
+        be.drift(0.01)
+        be.compute_forces(p, False)
+        be.kick(0.005)
+    out = be.download()
+    assert len(out) == len(b)
+    assert np.array_equal(np.sort(out.id), np.arange(len(b), dtype=np.uint32))
+    assert np.isfinite(out.x).all() and np.isfinite(out.vx).all()
+    assert np.array_equal(out.m, b.m[out.id])
+
+
+def test_theta0_exact_with_duplicate_keys(be):
+    b = S.cube(3000, 9)
+    b.x[:200] = 0.25
+    b.y[:200] = -0.5
+    b.z[:200] = 0.125
+    exact = O.direct_fp64(b, 1.0, 0.05)
+    ref_pe = 0.5 * float((b.m.astype(np.float64) * exact[3]).sum())
+    for bk in (be, with_env({"LETTUCE_CUDA_GROUP": "32"})):
+        g = accel(bk, b, params(1, 0.05, 0.0), True)
+        assert rel_rms(g.a, by_id(b.id, exact[:3])) <= 1e-5
+        assert g.times.interactions == 3000 * 2999
+        assert abs(g.diag.pe / ref_pe - 1) <= 1e-5
+
+
+def test_far_escaper_key_restart(be):
+    base = S.plummer(20000, 10, cut=20)
+    esc = L.Bodies.from_arrays(np.array([[1e8, 0, 0]]), np.zeros((1, 3)), np.array([base.m[0]], np.float64))
+    b = base.append(esc)
+    n = len(base)
+    p = params(1, 0.01, 0.6)
+    exact = O.direct_fp64(b, 1.0, 0.01)
+    ref_pe = 0.5 * float((b.m.astype(np.float64) * exact[3]).sum())
+    plain = accel(be, base, p, False)
+    g = accel(be, b, p, True)
+    e = rel_rms(g.a, by_id(b.id, exact[:3]))
+    print(f"escaper rel rms {e:.3g}, {g.times.interactions / (n + 1):.1f} int/body "
+          f"(without {plain.times.interactions / n:.1f}), build {g.times.build_ms:.3f} ms")
+    assert np.isfinite(g.a).all()
+    assert e <= 1e-3
+    assert abs(g.diag.pe / ref_pe - 1) <= 1e-3
+    assert g.times.interactions <= 2 * plain.times.interactions + 2 * (n + 1)
+    be.upload(b)
+    be.compute_forces(p, False)
+    for _ in range(3):
+        be.kick(0.005)
+        be.drift(0.01)
+        be.compute_forces(p, False)
+        be.kick(0.005)
+    out = be.download()
+    assert np.array_equal(np.sort(out.id), np.arange(len(b), dtype=np.uint32))
+
+
+def test_escaper_and_coincident_theta0_exact(be):
+    b = S.cube(3000, 11)
+    b.x[:100] = 0.25
+    b.y[:100] = -0.5
+    b.z[:100] = 0.125
+    b = b.append(L.Bodies.from_arrays(np.array([[1e8, 0, 0]]), np.zeros((1, 3)), np.array([b.m[0]], np.float64)))
+    N = len(b)
+    exact = O.direct_fp64(b, 1.0, 0.05)
+    ref_pe = 0.5 * float((b.m.astype(np.float64) * exact[3]).sum())
+    for theta in (0.0, 0.6):
+        g = accel(be, b, params(1, 0.05, theta), True)
+        e = rel_rms(g.a, by_id(b.id, exact[:3]))
+        assert np.isfinite(g.a).all()
+        if theta == 0.0:
+            assert e <= 1e-5
+            assert g.times.interactions == N * (N - 1)
+            assert abs(g.diag.pe / ref_pe - 1) <= 1e-5
+        else:
+            assert e <= 1e-2
+            assert abs(g.diag.pe / ref_pe - 1) <= 2e-4
+
+
+def test_build_tree_invalidates_and_split_call_is_bit_identical(be):
+    b = S.plummer(5000, 12, cut=20)
+    p = params(1, 0.01, 0.6)
+    be.upload(b)
+    be.compute_forces(p, True)
+    a1 = be.accel().copy()
+    ids1 = be.download().id.copy()
+    assert be.diagnostics().has_pe
+    be.build_tree(p)
+    assert not be.diagnostics().has_pe
+    with pytest.raises(L.LogicError):
+        be.kick(0.01)
+    be.compute_forces_with(p, True)
+    assert be.diagnostics().has_pe
+    assert np.array_equal(be.download().id, ids1)
+    assert np.array_equal(be.accel(), a1)
+    be.kick(0.01)
+    be.drift(0.01)
+    with pytest.raises(L.LogicError):
+        be.compute_forces_with(p, False)
+
+
+def test_one_million_body_tree_force_call(be):
+    n = 1 << 20
+    b = S.plummer(n, 6, cut=20)
+    p = params(1, 0.01, 0.6)
+    g = accel(be, b, p, False)
+    assert np.isfinite(g.a).all() and np.abs(g.a).max() > 0
+    be.compute_forces(p, False)
+    t = be.times()
+    print(f"1M tree: force {t.force_ms:.2f} ms (sort {t.sort_ms:.2f}, build {t.build_ms:.2f}, walk {t.walk_ms:.2f}),"
+          f" {t.interactions / n:.1f} interactions/body")
