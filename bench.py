@@ -1,0 +1,345 @@
+"""Benchmark of the GB300 engine on the reference's headline workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload disk1m|plummer16k]
+
+Workload (default, disk1m): the plain Barnes-Hut step with quadrupoles, theta 0.6, leaf <= 16,
+N = 1e6 exponential disk (sech^2 vertical profile, scale height 0.1, R <= 10, disk mass 1, central
+point mass 1), eps 0.005, dt 5e-4; one step = kick(dt/2), drift(dt), compute_forces, kick(dt/2)
+through the engine's C ABI (the reference's lettuce-bench step, src/bench.cpp:174-181). Seeded
+synthetic initial conditions; FP32 pair arithmetic, FP64 positions.
+
+Prints one JSON line. value = mean device time per step (CUDA events on the engine stream, L2
+flushed between steps outside the timed events); e2e = the same step through the public API with
+host buffers: upload of the state from page-locked memory, the step, download of the state.
+--impl reference times the reference CPU algorithm on the host's cores: the reference's own
+backend when it was built here from its sources (oracle/_ref), else the CPU oracle port.
+With --gpus N > 1 (torchrun) every rank runs an independent replica (the single-system step does
+not shard without the multi-rank tree exchange, which is out of scope); value is the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/step N=1e6 tree θ=0.6 at ≤1e-3 force err; adjoint÷forward, batched÷plain"
+
+WORKLOADS = {
+    "disk1m": dict(kind="disk", n=1_000_000, seed=1, eps=0.005, dt=5e-4, theta=0.6, method="tree",
+                   desc="BH quadrupole tree, theta 0.6, leaf<=16, N=1e6 exponential disk (sech^2 h=0.1, R<=10, "
+                        "core mass 1), eps 0.005, dt 5e-4"),
+    "plummer16k": dict(kind="plummer", n=16384, seed=1, eps=0.01, dt=1e-3, theta=0.6, method="direct",
+                       desc="direct summation, N=16384 Plummer (Henon units, r<10a), eps 0.01, dt 1e-3"),
+}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def make_bodies(w):
+    from lettuce_simulate_physics_gb300 import scenarios as S
+    if w["kind"] == "disk":
+        return S.disk(w["n"], w["seed"])
+    return S.plummer(w["n"], w["seed"], cut=10.0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def force_error_sample(be, b, w, count=256, seed=7):
+    """Median and 99th-percentile per-body relative error of the engine's accelerations against an
+    FP64 direct sum over all N bodies, for a seeded sample of bodies (numpy, chunked)."""
+    a = be.accel()
+    ids = be.download().id
+    n = len(ids)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pick = rng.choice(n, size=min(count, n), replace=False)
+    pos = be.pos64().T
+    m = be.download().m.astype(np.float64)
+    e2 = w["eps"] ** 2
+    errs = []
+    for s in range(0, len(pick), 8):
+        idx = pick[s:s + 8]
+        d = pos[None, :, :] - pos[idx][:, None, :]
+        r2 = (d * d).sum(-1) + e2
+        r2[np.arange(len(idx)), idx] = np.inf
+        inv3 = r2 ** -1.5
+        ref = (d * (m[None, :] * inv3)[..., None]).sum(1)
+        got = a[:3, idx].T.astype(np.float64)
+        errs.extend((np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)).tolist())
+    return float(np.median(errs)), float(np.percentile(errs, 99))
+
+
+def read_profile_traffic(workload):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_port_steps(b, w, steps, threads=0):
+    """The reference CPU algorithm (oracle/_ref if built from the reference, else the port):
+    `steps` KDK steps after one warm-up force call; returns (ms/step, kind, threads)."""
+    from oracle import oracle as O
+    O.build()
+    kind = "ref" if O.available("ref") else "port"
+    cpu = O.OracleBackend(kind, threads)
+    method = O.TREE if w["method"] == "tree" else O.DIRECT
+    cpu.upload(b)
+    cpu.compute_forces(method, 1.0, w["eps"], w["theta"], False)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        cpu.kick(0.5 * w["dt"])
+        cpu.drift(w["dt"])
+        cpu.compute_forces(method, 1.0, w["eps"], w["theta"], False)
+        cpu.kick(0.5 * w["dt"])
+    ms = (time.perf_counter() - t0) * 1e3 / max(steps, 1)
+    nt = cpu.threads()
+    cpu.close()
+    return ms, ("reference" if kind == "ref" else "port"), int(nt)
+
+
+def run_reference(args, w, world, rank, dist):
+    if rank != 0:
+        return 0
+    b = make_bodies(w)
+    steps = max(1, args.steps)
+    # Bounded sample: the full-N step, as many as the budget allows (at least one).
+    ms, kind, threads = cpu_port_steps(b, w, min(steps, args.ref_steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": args.gpus,
+        "steps": min(steps, args.ref_steps), "warmup": 1, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f32-positions", "data": "synthetic (seeded)",
+        "config": {"workload": w["desc"], "n": w["n"], "method": w["method"], "theta": w["theta"]},
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
+                         "sample": f"{min(steps, args.ref_steps)} KDK steps of the full workload (N={w['n']})"},
+        "e2e": {"value": round(ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, w, world, rank, local, dist):
+    import lettuce_simulate_physics_gb300 as L
+    from lettuce_simulate_physics_gb300 import build as B
+    from lettuce_simulate_physics_gb300.backend import PinnedBodies
+    B.build()
+    b = make_bodies(w)
+    n = len(b)
+    be = L.CudaBackend(local)
+    method = L.ForceMethod.tree if w["method"] == "tree" else L.ForceMethod.direct
+    p = L.ForceParams(G=1.0, eps=w["eps"], theta=w["theta"], method=method)
+    dt = w["dt"]
+    be.upload(b)
+    be.compute_forces(p, False)
+    err_med, err_p99 = force_error_sample(be, b, w)
+
+    def step():
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        be.kick(0.5 * dt)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    be.synchronize()
+    walk_ms, sort_ms, build_ms, force_ms, step_ms, inter, pairs, cells = [], [], [], [], [], [], [], []
+    barrier(dist)
+    launches0 = be.launch_count()
+    with ClockSampler(local) as clk:
+        be.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            be.flush_l2()
+            be.event_record(0)
+            step()
+            be.event_record(1)
+            step_ms.append(be.event_elapsed(0, 1))
+            t = be.times()
+            walk_ms.append(t.walk_ms)
+            sort_ms.append(t.sort_ms)
+            build_ms.append(t.build_ms)
+            force_ms.append(t.force_ms)
+            inter.append(t.interactions)
+            bp, ct = be.interaction_split()
+            pairs.append(bp)
+            cells.append(ct)
+        be.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    launches = be.launch_count() - launches0
+    ms = reduce_max(dist, statistics.fmean(step_ms))
+    clocks = clk.summary()
+
+    # Roofline of the dominant kernel (the walk): algorithmic flops / walk time.
+    # 20 flops per body-body pair, 65 per quadrupole cell term (per-unit counts in the design doc).
+    if method == L.ForceMethod.tree:
+        flops = [20.0 * a + 65.0 * c for a, c in zip(pairs, cells)]
+    else:
+        flops = [20.0 * a for a in pairs]
+    achieved = statistics.fmean([f / (t_ms * 1e-3) / 1e12 for f, t_ms in zip(flops, walk_ms)])
+    peak = be.probe_fp32_peak()
+    traffic = read_profile_traffic(args.workload)
+
+    # End to end through the public API with host buffers: upload from page-locked memory, one
+    # step, download of the state, each step.
+    pin = PinnedBodies(n)
+    hb = pin.bodies
+    for f in ("x", "y", "z", "vx", "vy", "vz", "m", "id"):
+        getattr(hb, f)[:] = getattr(b, f)
+    e2e_steps = max(1, min(args.steps, 10))
+    be.upload(hb)
+    be.compute_forces(p, False)
+    be.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        be.upload(hb)
+        be.compute_forces(p, False)
+        step()
+        be.download()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    pin.free()
+    e2e_ms = reduce_max(dist, e2e_ms)
+
+    # CPU baseline (rank 0, N=1): the reference CPU algorithm on this host's cores, bounded sample.
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cms, kind, threads = cpu_port_steps(b, w, args.ref_steps)
+        cpu = {"value": round(cms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
+               "sample": f"{args.ref_steps} KDK step(s) of the full workload (N={n}) after one warm-up force call"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-positions", "data": "synthetic (seeded)",
+            "config": {"workload": w["desc"], "n": n, "method": w["method"], "theta": w["theta"],
+                       "parallelism": "replicas" if world > 1 else "single-gpu",
+                       "l2": "flushed between timed steps (write of 2x L2 outside the step events)"},
+            "phases_ms": {"sort": round(statistics.fmean(sort_ms), 4), "build": round(statistics.fmean(build_ms), 4),
+                          "walk": round(statistics.fmean(walk_ms), 4), "force": round(statistics.fmean(force_ms), 4)},
+            "interactions_per_step": int(statistics.fmean(inter)),
+            "ginteractions_per_s": round(statistics.fmean(inter) / (statistics.fmean(force_ms) * 1e-3) / 1e9, 2),
+            "force_error_vs_fp64": {"median": err_med, "p99": err_p99, "sample_bodies": 256},
+            "roofline": {"bound": "fp32", "kernel": "walk" if method == L.ForceMethod.tree else "direct",
+                         "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+                         "frac": round(achieved / peak, 4) if peak else None, "traffic": traffic,
+                         "peak_source": "measured FFMA throughput on this GPU (lg_probe_fp32_peak)",
+                         "flops_per_unit": {"body_pair": 20, "cell_term": 65}},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 32 * n,
+                    "d2h_bytes_per_step": 32 * n},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    be.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="disk1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--ref-steps", type=int, default=2, help="KDK steps timed on the CPU")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, w, world, rank, dist)
+    return run_gb300(args, w, world, rank, local, dist)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

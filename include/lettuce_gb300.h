@@ -152,6 +152,16 @@ lg_status lg_synchronize(lg_engine* e);
 lg_status lg_flush_l2(lg_engine* e);
 /* Number of engine kernel launches issued so far (a counter kept by the host side). */
 lg_status lg_launch_count(const lg_engine* e, uint64_t* count);
+/* Split of the last force call's interactions: body-body pairs and body-cell (quadrupole) terms;
+ * body_pairs + cell_terms == interactions. For the direct method cell_terms = 0. */
+lg_status lg_interaction_split(lg_engine* e, uint64_t* body_pairs, uint64_t* cell_terms);
+/* Measured FP32 FMA throughput of this device (a dependent-free FFMA loop over every SM, timed
+ * with CUDA events on the engine's stream), in TFLOP/s: the roofline denominator of the force
+ * kernels. */
+lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops);
+/* Page-locked host memory for transfers that overlap (cudaMallocHost / cudaFreeHost). */
+lg_status lg_host_alloc(size_t bytes, void** out);
+lg_status lg_host_free(void* p);
 
 #ifdef __cplusplus
 }

@@ -162,6 +162,10 @@ def _lib() -> C.CDLL:
         "lg_synchronize": (st, [vp]),
         "lg_flush_l2": (st, [vp]),
         "lg_launch_count": (st, [vp, C.POINTER(C.c_uint64)]),
+        "lg_interaction_split": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+        "lg_probe_fp32_peak": (st, [vp, C.POINTER(C.c_double)]),
+        "lg_host_alloc": (st, [C.c_size_t, C.POINTER(vp)]),
+        "lg_host_free": (st, [vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -372,10 +376,44 @@ class CudaBackend:
     def flush_l2(self) -> None:
         _check(self._lib.lg_flush_l2(self._h))
 
+    def interaction_split(self):
+        """(body pairs, cell terms) of the last force call."""
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(self._lib.lg_interaction_split(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
+    def probe_fp32_peak(self) -> float:
+        t = C.c_double()
+        _check(self._lib.lg_probe_fp32_peak(self._h, C.byref(t)))
+        return float(t.value)
+
     def launch_count(self) -> int:
         c = C.c_uint64()
         _check(self._lib.lg_launch_count(self._h, C.byref(c)))
         return int(c.value)
+
+
+class PinnedBodies:
+    """Bodies whose arrays live in page-locked host memory (lg_host_alloc), for transfers at full
+    PCIe/C2C bandwidth. Call free() when done."""
+
+    def __init__(self, n: int):
+        lib = _lib()
+        self._ptr = C.c_void_p()
+        _check(lib.lg_host_alloc(max(n, 1) * 32, C.byref(self._ptr)))
+        buf = (C.c_char * (max(n, 1) * 32)).from_address(self._ptr.value)
+        raw = np.frombuffer(buf, dtype=np.uint8)
+        cols = [raw[k * 4 * max(n, 1):(k + 1) * 4 * max(n, 1)] for k in range(8)]
+        f = [c.view(np.float32)[:n] for c in cols[:7]]
+        self.bodies = Bodies.__new__(Bodies)
+        for name, arr in zip(("x", "y", "z", "vx", "vy", "vz", "m"), f):
+            setattr(self.bodies, name, arr)
+        self.bodies.id = cols[7].view(np.uint32)[:n]
+
+    def free(self):
+        if self._ptr:
+            _lib().lg_host_free(self._ptr)
+            self._ptr = None
 
 
 def make_cuda_backend(device: int = 0):

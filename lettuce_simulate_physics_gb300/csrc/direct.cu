@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
                 const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
                 float inv = rsqrt_mufu(r2);
                 if (EPS0) inv = r2 > 0.f ? inv : 0.f;
-                const float mi = q.w * inv;
+                const float mi = __fmul_rn(q.w, inv);  // rounded: the self term cancels exactly
                 const float f = mi * (inv * inv);
                 px[u] = __fmaf_rn(f, dx, px[u]);
                 py[u] = __fmaf_rn(f, dy, py[u]);
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
         float p = sp[u] - cp[u];
         if (POT && !EPS0 && i >= j0 && i < j1) {
             // The self pair's potential term, exactly as the loop formed it (r2 == e2).
-            p -= mself[u] * rsqrt_mufu(e2);
+            p = __fsub_rn(p, __fmul_rn(mself[u], rsqrt_mufu(e2)));
         }
         if (write_final)
             out[i] = make_float4(G * (sx[u] - cx[u]), G * (sy[u] - cy[u]), G * (sz[u] - cz[u]), POT ? -G * p : 0.f);

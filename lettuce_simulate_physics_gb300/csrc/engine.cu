@@ -234,8 +234,11 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
     pend_tree_times = false;
     times.walk_ms = elapsed(EV_WALK0, EV_WALK1);
     times.force_ms = times.sort_ms + times.build_ms + times.walk_ms;
-    const unsigned long long counted = *reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(pinned_small) + 64);
-    times.interactions = tree_m ? counted : static_cast<uint64_t>(n) * static_cast<uint64_t>(n - 1);
+    const unsigned long long* cnt = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(pinned_small) + 64);
+    // Walk: [0] body pairs (own entry excluded), [1] cell terms.
+    last_body_pairs = tree_m ? cnt[0] : static_cast<uint64_t>(n) * static_cast<uint64_t>(n - 1);
+    last_cell_terms = tree_m ? cnt[1] : 0;
+    times.interactions = last_body_pairs + last_cell_terms;
     has_pe = potential;
     acc_ok = true;
     costs_ok = true;
@@ -635,6 +638,39 @@ lg_status lg_synchronize(lg_engine* e) {
 }
 
 lg_status lg_flush_l2(lg_engine* e) { return guard([&] { eng(e).flush_l2(); }); }
+
+lg_status lg_interaction_split(lg_engine* e, uint64_t* body_pairs, uint64_t* cell_terms) {
+    return guard([&] {
+        need(body_pairs, "body_pairs");
+        need(cell_terms, "cell_terms");
+        Engine& E = eng(e);
+        *body_pairs = E.last_body_pairs;
+        *cell_terms = E.last_cell_terms;
+    });
+}
+
+lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops) {
+    return guard([&] {
+        need(tflops, "tflops");
+        Engine& E = eng(e);
+        LG_CK(cudaSetDevice(E.dev));
+        *tflops = lg::probe_fp32_peak(E.stream, E.sms, E.err_word() + 12);
+    });
+}
+
+lg_status lg_host_alloc(size_t bytes, void** out) {
+    return guard([&] {
+        need(out, "out");
+        *out = nullptr;
+        LG_CK(cudaMallocHost(out, bytes ? bytes : 1));
+    });
+}
+
+lg_status lg_host_free(void* p) {
+    return guard([&] {
+        if (p) LG_CK(cudaFreeHost(p));
+    });
+}
 
 lg_status lg_launch_count(const lg_engine* e, uint64_t* count) {
     return guard([&] {

@@ -93,6 +93,7 @@ struct Engine {
     bool kick_rec = false, drift_rec = false, pend_tree_times = false;
     lg_phase_times times{};
     uint64_t launches = 0;
+    uint64_t last_body_pairs = 0, last_cell_terms = 0;
     std::unique_ptr<TreeState, void (*)(TreeState*)> tree{nullptr, nullptr};
 };
 
@@ -112,5 +113,7 @@ lg_memory_estimate memory_need(uint64_t n, int method);
 const void* probe_kernel();
 // walk.cu
 void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0);
+// integrate.cu
+double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink);
 
 }  // namespace lg

@@ -1,5 +1,7 @@
 // Integration and reduction kernels: upload widening, download rounding, FP32 kick, FP64 drift,
 // FP64 diagnostics and bounds, the exact FP64 potential energy, and utility kernels.
+#include <algorithm>
+
 #include "lg_engine.cuh"
 
 namespace lg {
@@ -223,7 +225,47 @@ __global__ void k_flush(float* __restrict__ a, size_t count) {
         a[i] = a[i] * 0.5f + 1.f;
 }
 
+// FP32 FMA throughput probe: 8 independent FFMA chains per thread, no memory traffic in the loop.
+__global__ void k_ffma_probe(int iters, float seed, unsigned* sink) {
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = seed + threadIdx.x * 1e-7f + k;
+    const float b = 0.999999f, c = 1e-7f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = __fmaf_rn(a[k], b, c);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == 12345.678f) atomicAdd(sink, 1u);  // keeps the chains live
+}
+
 }  // namespace
+
+double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink) {
+    const int blocks = sms * 8, threads = 256, iters = 1 << 14;
+    cudaEvent_t a, b;
+    LG_CK(cudaEventCreate(&a));
+    LG_CK(cudaEventCreate(&b));
+    k_ffma_probe<<<blocks, threads, 0, s>>>(iters, 1.f, sink);  // warm-up
+    LG_LAUNCHED();
+    double best = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+        LG_CK(cudaEventRecord(a, s));
+        k_ffma_probe<<<blocks, threads, 0, s>>>(iters, 1.f + rep, sink);
+        LG_LAUNCHED();
+        LG_CK(cudaEventRecord(b, s));
+        LG_CK(cudaEventSynchronize(b));
+        float ms = 0;
+        LG_CK(cudaEventElapsedTime(&ms, a, b));
+        const double flops = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads;
+        best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return best;
+}
 
 void launch_widen(const float* x, const float* y, const float* z, const float* m, BodyArrays b, int n, cudaStream_t s) {
     if (n <= 0) return;

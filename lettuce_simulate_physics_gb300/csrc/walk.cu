@@ -131,7 +131,7 @@ __device__ __forceinline__ void eval_bodies(const WarpSmem& s, int bc, const flo
             const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
             float inv = rsqrt_mufu(r2);
             if (EPS0) inv = r2 > 0.f ? inv : 0.f;
-            const float mi = q.w * inv;
+            const float mi = __fmul_rn(q.w, inv);  // rounded: the self term cancels exactly
             const float f = mi * (inv * inv);
             a.px[u] = __fmaf_rn(f, dx, a.px[u]);
             a.py[u] = __fmaf_rn(f, dy, a.py[u]);
@@ -198,7 +198,7 @@ __device__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int nc, int nr, 
 
 template <int IPT, bool POT, bool EPS0>
 __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int lane, uint2 gr, float4 bc, float4 bh,
-                          uint32_t plo, int np, unsigned long long& inter) {
+                          uint32_t plo, int np, unsigned long long& inter_b, unsigned long long& inter_c) {
     const float ox = bc.x, oy = bc.y, oz = bc.z;
     float xi[IPT], yi[IPT], zi[IPT], mi[IPT];
 #pragma unroll
@@ -217,7 +217,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     if (lane == 0) stack[0] = 0;
     __syncwarp();
     int nc = 0, nr = 0, nbr = 0;
-    uint32_t list_len = 0;
+    uint32_t list_len = 0, cells_len = 0;
     bool overflow = false;
     // Each node is visited at most once per pass; the cap stops a malformed tree.
     const uint32_t max_iter = static_cast<uint32_t>(w.tv.T) + 64u;
@@ -278,6 +278,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         if (nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
             flush<IPT, POT, EPS0>(w, s, lane, nc, nr, ox, oy, oz, xi, yi, zi, a);
             list_len += nc + nbr;
+            cells_len += nc;
             nc = nr = nbr = 0;
         }
     }
@@ -286,6 +287,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     } else {
         flush<IPT, POT, EPS0>(w, s, lane, nc, nr, ox, oy, oz, xi, yi, zi, a);
         list_len += nc + nbr;
+        cells_len += nc;
     }
     const float self_inv = (POT && !EPS0) ? rsqrt_mufu(w.e2) : 0.f;
 #pragma unroll
@@ -296,12 +298,13 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         float p = a.sp[u] - a.cp[u];
         // The own body is always in the list (its leaf is inside the group, so it is opened);
         // with eps > 0 its pair has d = 0 and only adds m_i/eps to the potential.
-        if (POT && !EPS0) p -= mi[u] * self_inv;
+        if (POT && !EPS0) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
         w.acc[i] = make_float4(w.G * (a.sx[u] - a.cx[u]), w.G * (a.sy[u] - a.cy[u]), w.G * (a.sz[u] - a.cz[u]),
                                POT ? -w.G * p : 0.f);
         w.cost[i] = static_cast<float>(list_len - 1);
     }
-    inter += static_cast<unsigned long long>(list_len - 1) * static_cast<unsigned long long>(np);
+    inter_b += static_cast<unsigned long long>(list_len - cells_len - 1) * static_cast<unsigned long long>(np);
+    inter_c += static_cast<unsigned long long>(cells_len) * static_cast<unsigned long long>(np);
 }
 
 template <bool POT, bool EPS0>
@@ -311,7 +314,7 @@ __global__ void __launch_bounds__(WBS) k_walk(WalkArgs w) {
     WarpSmem& s = sm[wid];
     uint32_t* stack = w.stack + (static_cast<size_t>(blockIdx.x) * WARPS + wid) * SCAP;
     const unsigned ngroups = *w.tv.ngroups;
-    unsigned long long inter = 0;
+    unsigned long long inter_b = 0, inter_c = 0;
     for (;;) {
         unsigned g = 0;
         if (lane == 0) g = atomicAdd(w.group_ctr, 1u);
@@ -322,14 +325,17 @@ __global__ void __launch_bounds__(WBS) k_walk(WalkArgs w) {
         for (uint32_t plo = gr.x; plo < gr.y; plo += PASS) {
             const int np = static_cast<int>(min(static_cast<uint32_t>(PASS), gr.y - plo));
             switch ((np + 31) >> 5) {
-                case 1: walk_pass<1, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter); break;
-                case 2: walk_pass<2, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter); break;
-                case 3: walk_pass<3, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter); break;
-                default: walk_pass<4, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter); break;
+                case 1: walk_pass<1, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
+                case 2: walk_pass<2, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
+                case 3: walk_pass<3, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
+                default: walk_pass<4, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
             }
         }
     }
-    if (lane == 0 && inter) atomicAdd(w.inter, inter);
+    if (lane == 0) {
+        if (inter_b) atomicAdd(w.inter, inter_b);
+        if (inter_c) atomicAdd(w.inter + 1, inter_c);
+    }
 }
 
 template <bool POT, bool EPS0>

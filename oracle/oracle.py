@@ -88,6 +88,8 @@ def _lib(kind: str) -> C.CDLL:
         "get_keys": (None, [vp, C.POINTER(C.c_uint64)]),
         "get_frame": (None, [vp, _d]),
     }
+    if kind == "port":
+        sig["threads"] = (C.c_int, [vp])
     for name, (res, args) in sig.items():
         fn = getattr(lib, p + name)
         fn.restype = res
@@ -131,6 +133,13 @@ class OracleBackend:
 
     def _call(self, name, *args):
         return getattr(self._lib, self._p + name)(*args)
+
+    def threads(self) -> int:
+        """Host threads the backend uses."""
+        if self.kind == "port":
+            return int(self._call("threads", self._h))
+        import os
+        return os.cpu_count() or 1
 
     def close(self):
         if self._h:
