@@ -163,6 +163,22 @@ lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops);
 lg_status lg_host_alloc(size_t bytes, void** out);
 lg_status lg_host_free(void* p);
 
+/* Direct-summation forces with no device allocation. No counterpart in the reference: it is for
+ * callers that cannot allocate device memory when they need forces, such as a code that owns all
+ * device memory through its own fixed arena, or a stepping loop that must avoid cudaMalloc's
+ * implicit device synchronisation. The caller passes device arrays: posm[n] float4 (x, y, z, m)
+ * and poslo[n] float4 (low parts of FP64 positions, or zeros), and receives acc[n] float4
+ * (ax, ay, az, phi; phi only with potential != 0) on its stream (a cudaStream_t, NULL for the
+ * legacy stream). The call synchronises that stream before it returns.
+ * Scratch is a static device array inside this library (16 MiB of split-j partial sums plus a
+ * status word), held by every GPU that loads the library until the process exits; n above
+ * 1,048,576 is rejected with LG_ERR_ARG. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, which loads the module): make that first call before any stream
+ * capture. All calls share the array and it keeps the last call's contents, so calls that
+ * overlap on the GPU (other streams, other host threads) race and must not be issued. */
+lg_status lg_direct_forces_noalloc(const void* posm, const void* poslo, int n, double G, double eps, int potential,
+                                   void* acc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

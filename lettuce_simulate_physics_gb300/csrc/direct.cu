@@ -13,7 +13,9 @@
 // Self interaction: with eps > 0 the self pair has d = 0 exactly (same relative coordinates), so
 // it adds nothing to a; its potential term m_i/eps is subtracted at the end. With eps == 0 the
 // r2 > 0 guard drops self and coincident pairs, as the reference does.
-#include "lg_engine.cuh"
+#include <mutex>
+
+#include "engine.cuh"
 
 namespace lg {
 
@@ -225,4 +227,93 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
     }
 }
 
+
+// ---- Entry point without device allocation ---------------------------------------------------
+// Some callers cannot call cudaMalloc at the point where they need forces: a code that owns all
+// device memory through its own fixed arena, or a time-stepping loop that must not hit
+// cudaMalloc's implicit device synchronisation between steps. lg_direct_forces_noalloc serves
+// them: the caller passes device inputs and outputs, and the split-j scratch lives in the static
+// array below instead of an engine buffer.
+namespace {
+
+constexpr size_t kNoAllocStatusBytes = 256;
+constexpr size_t kNoAllocPartials = size_t(1) << 20;  // float4 entries (16 MiB)
+constexpr int kNoAllocMaxN = 1 << 20;
+constexpr int kNoAllocMaxDevices = 64;
+
+// Status words, then split-j partial sums. Part of the library image: every GPU that loads the
+// library holds these 16 MiB until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocStatusBytes + kNoAllocPartials * 16];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch for the current device, looked up once per device. The
+// host-side name is only a stand-in; kernels must be given this address.
+unsigned char* noalloc_scratch(int dev) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            fail(kRuntime, std::string("lg_direct_forces_noalloc: cudaGetSymbolAddress failed: ") +
+                               cudaGetErrorString(e));
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    return static_cast<unsigned char*>(g_noalloc_addr[dev]);
+}
+
+}  // namespace
+
 }  // namespace lg
+
+extern "C" lg_status lg_direct_forces_noalloc(const void* posm, const void* poslo, int n, double G, double eps,
+                                              int potential, void* acc, void* stream) {
+    try {
+        if (n < 0 || n > lg::kNoAllocMaxN)
+            lg::fail(lg::kArg, "lg_direct_forces_noalloc: n = " + std::to_string(n) + " is outside [0, " +
+                                   std::to_string(lg::kNoAllocMaxN) + "], the size its static scratch serves");
+        if (n > 0 && (!posm || !poslo || !acc)) lg::fail(lg::kArg, "lg_direct_forces_noalloc: null device pointer");
+        if (n == 0) {
+            lg::g_last_error.clear();
+            return LG_OK;
+        }
+        int dev = 0;
+        LG_CK(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= lg::kNoAllocMaxDevices) lg::fail(lg::kArg, "lg_direct_forces_noalloc: device index too large");
+        int sms = 0;
+        LG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        unsigned char* base = lg::noalloc_scratch(dev);
+        unsigned* err = reinterpret_cast<unsigned*>(base);
+        float4* partial = reinterpret_cast<float4*>(base + lg::kNoAllocStatusBytes);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        lg::DirectShape sh = lg::default_direct_shape(n, sms);
+        const long long cap = static_cast<long long>(lg::kNoAllocPartials) / n;
+        if (sh.slices > cap) sh.slices = static_cast<int>(cap < 1 ? 1 : cap);
+        lg::BodyArrays b;
+        b.hm = const_cast<float4*>(static_cast<const float4*>(posm));
+        b.lo = const_cast<float4*>(static_cast<const float4*>(poslo));
+        const float e2 = static_cast<float>(eps * eps);
+        const bool eps0 = !(e2 >= 1.17549435e-38f);
+        // The array keeps the previous call's contents: the status word must start at zero; the
+        // partial sums are overwritten before they are read.
+        LG_CK(cudaMemsetAsync(err, 0, sizeof(unsigned), s));
+        lg::launch_direct(b, n, static_cast<float>(G), e2, potential != 0, eps0, sh, static_cast<float4*>(acc), partial,
+                          err, s);
+        unsigned h_err = 0;
+        LG_CK(cudaMemcpyAsync(&h_err, err, sizeof h_err, cudaMemcpyDeviceToHost, s));
+        LG_CK(cudaStreamSynchronize(s));
+        if (h_err) lg::fail(lg::kRuntime, "lg_direct_forces_noalloc: device wait timed out; accelerations are invalid");
+        lg::g_last_error.clear();
+        return LG_OK;
+    } catch (const lg::Error& ex) {
+        lg::g_last_error = ex.what();
+        return static_cast<lg_status>(ex.status);
+    } catch (const std::exception& ex) {
+        lg::g_last_error = ex.what();
+        return LG_ERR_RUNTIME;
+    }
+}
+
