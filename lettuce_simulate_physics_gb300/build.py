@@ -40,9 +40,9 @@ def _headers_mtime() -> float:
 def _compile(src: str, verbose: bool, ptxas_v: bool) -> str:
     obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
     newest = max(os.path.getmtime(src), _headers_mtime())
-    if os.path.exists(obj) and os.path.getmtime(obj) >= newest and not ptxas_v:
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest and not ptxas_v and not os.environ.get("LG_NVCC_EXTRA"):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *os.environ.get("LG_NVCC_EXTRA", "").split(), "-c", src, "-o", obj]
     if ptxas_v:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

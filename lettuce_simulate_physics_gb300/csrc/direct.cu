@@ -6,13 +6,16 @@
 //    stages, so the copy of tile t+2 overlaps the arithmetic on tile t;
 //  - each tile is converted once per block to coordinates relative to the block origin o (the
 //    first i-body): (x_hi - o_hi) + (x_lo - o_lo) in FP32, so close pairs keep the FP64
-//    separation and the inner loop is plain FP32 (3 FADD, 3 FFMA, 1 MUFU.RSQ, 3 FMUL, 3 FFMA);
+//    separation; the converted tile is struct-of-arrays, so j-bodies k, k+1 load as one float2
+//    and the inner loop evaluates both with packed f32x2 instructions (per two pairs: 3 FADD2,
+//    3 FFMA2, 2 MUFU.RSQ, 3 FMUL2, 3 FFMA2 -- half the issue slots of the scalar loop);
 //  - per-tile partial sums are added to the running sums with Kahan compensation;
 //  - small N splits the j range over blockIdx.y (split-j); the slices' partials are summed in a
 //    fixed order by a second kernel, so results do not depend on scheduling.
 // Self interaction: with eps > 0 the self pair has d = 0 exactly (same relative coordinates), so
 // it adds nothing to a; its potential term m_i/eps is subtracted at the end. With eps == 0 the
 // r2 > 0 guard drops self and coincident pairs, as the reference does.
+#include <algorithm>
 #include <mutex>
 
 #include "engine.cuh"
@@ -27,7 +30,7 @@ constexpr int TILE = 256;  // j-bodies per stage
 struct alignas(16) DirectSmem {
     float4 raw_hm[2][TILE];
     float4 raw_lo[2][TILE];
-    float4 rel[2][TILE];
+    float rx[2][TILE], ry[2][TILE], rz[2][TILE], rm[2][TILE];
     uint64_t bar[2];
 };
 
@@ -60,6 +63,15 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
         cx[u] = cy[u] = cz[u] = cp[u] = 0.f;
     }
 
+    f2x XI[IPT], YI[IPT], ZI[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        XI[u] = f2_bcast(xi[u]);
+        YI[u] = f2_bcast(yi[u]);
+        ZI[u] = f2_bcast(zi[u]);
+    }
+    const f2x E2 = f2_bcast(e2);
+
     if (tid == 0) {
         mbar_init(&sm.bar[0], 1);
         mbar_init(&sm.bar[1], 1);
@@ -89,15 +101,19 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
         const int cnt8 = (cnt + 7) & ~7;
         if (ok) {
             for (int k = tid; k < cnt8; k += DBS) {
-                float4 r;
                 if (k < cnt) {
                     const float4 h = sm.raw_hm[buf][k], l = sm.raw_lo[buf][k];
-                    r = make_float4((h.x - oh.x) + (l.x - ol.x), (h.y - oh.y) + (l.y - ol.y),
-                                    (h.z - oh.z) + (l.z - ol.z), h.w);
+                    sm.rx[buf][k] = (h.x - oh.x) + (l.x - ol.x);
+                    sm.ry[buf][k] = (h.y - oh.y) + (l.y - ol.y);
+                    sm.rz[buf][k] = (h.z - oh.z) + (l.z - ol.z);
+                    sm.rm[buf][k] = h.w;
                 } else {
-                    r = make_float4(0.f, 0.f, 0.f, 0.f);  // zero mass at the origin adds nothing
+                    // A far, massless body: pads the tile and adds exactly zero.
+                    sm.rx[buf][k] = 1e18f;
+                    sm.ry[buf][k] = 1e18f;
+                    sm.rz[buf][k] = 1e18f;
+                    sm.rm[buf][k] = 0.f;
                 }
-                sm.rel[buf][k] = r;
             }
         }
         if (__syncthreads_or(!ok)) {
@@ -108,33 +124,43 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
             fence_proxy_async_smem();
             issue(t + 2);
         }
-        float px[IPT], py[IPT], pz[IPT], pp[IPT];
+        f2x px[IPT], py[IPT], pz[IPT], pp[IPT];
 #pragma unroll
-        for (int u = 0; u < IPT; ++u) px[u] = py[u] = pz[u] = pp[u] = 0.f;
-        const float4* rel = sm.rel[buf];
-#pragma unroll 4
-        for (int k = 0; k < cnt8; ++k) {
-            const float4 q = rel[k];
+        for (int u = 0; u < IPT; ++u) px[u] = py[u] = pz[u] = pp[u] = 0ull;
+        const float* rx = sm.rx[buf];
+        const float* ry = sm.ry[buf];
+        const float* rz = sm.rz[buf];
+        const float* rm = sm.rm[buf];
+#pragma unroll 1
+        for (int k = 0; k < cnt8; k += 2) {
+            const f2x X = *reinterpret_cast<const f2x*>(rx + k), Y = *reinterpret_cast<const f2x*>(ry + k);
+            const f2x Z = *reinterpret_cast<const f2x*>(rz + k), M = *reinterpret_cast<const f2x*>(rm + k);
 #pragma unroll
             for (int u = 0; u < IPT; ++u) {
-                const float dx = q.x - xi[u], dy = q.y - yi[u], dz = q.z - zi[u];
-                const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
-                float inv = rsqrt_mufu(r2);
-                if (EPS0) inv = r2 > 0.f ? inv : 0.f;
-                const float mi = __fmul_rn(q.w, inv);  // rounded: the self term cancels exactly
-                const float f = mi * (inv * inv);
-                px[u] = __fmaf_rn(f, dx, px[u]);
-                py[u] = __fmaf_rn(f, dy, py[u]);
-                pz[u] = __fmaf_rn(f, dz, pz[u]);
-                if (POT) pp[u] += mi;
+                const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+                const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+                float r2a, r2b;
+                f2_unpack(r2, r2a, r2b);
+                float ia = rsqrt_mufu(r2a), ib = rsqrt_mufu(r2b);
+                if (EPS0) {
+                    ia = r2a > 0.f ? ia : 0.f;
+                    ib = r2b > 0.f ? ib : 0.f;
+                }
+                const f2x inv = f2_pack(ia, ib);
+                const f2x mi = f2_mul(M, inv);  // rounded: the self term cancels exactly
+                const f2x f = f2_mul(mi, f2_mul(inv, inv));
+                px[u] = f2_fma(f, dx, px[u]);
+                py[u] = f2_fma(f, dy, py[u]);
+                pz[u] = f2_fma(f, dz, pz[u]);
+                if (POT) pp[u] = f2_add(pp[u], mi);
             }
         }
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-            kahan_add(sx[u], cx[u], px[u]);
-            kahan_add(sy[u], cy[u], py[u]);
-            kahan_add(sz[u], cz[u], pz[u]);
-            if (POT) kahan_add(sp[u], cp[u], pp[u]);
+            kahan_add(sx[u], cx[u], f2_sum(px[u]));
+            kahan_add(sy[u], cy[u], f2_sum(py[u]));
+            kahan_add(sz[u], cz[u], f2_sum(pz[u]));
+            if (POT) kahan_add(sp[u], cp[u], f2_sum(pp[u]));
         }
     }
     if (failed) {
@@ -193,16 +219,29 @@ void launch_ipt(const BodyArrays b, int n, float G, float e2, bool pot, bool eps
 
 }  // namespace
 
+// Default shape: i-bodies per thread by size, and a split-j count that makes the grid a whole
+// number of waves (blocks resident at once = SMs x blocks per SM), so no partial wave idles SMs.
 DirectShape default_direct_shape(int n, int sms) {
     DirectShape sh;
     sh.ipt = n >= 8 * 1024 ? 4 : (n >= 2048 ? 2 : 1);
     sh.tile = TILE;
     const int iblocks = (n + DBS * sh.ipt - 1) / (DBS * sh.ipt);
-    const int target = 3 * sms;  // about three resident blocks per SM
-    const int max_slices = (n + TILE - 1) / TILE;
-    int slices = (target + iblocks - 1) / iblocks;
-    slices = slices < 1 ? 1 : (slices > max_slices ? max_slices : slices);
-    sh.slices = slices;
+    const int wave = 2 * sms;  // two 256-thread blocks of the IPT-4 kernel fit per SM
+    const int max_slices = std::max(1, n / 128);
+    int best = 1;
+    double best_eff = 0;
+    for (int waves = 1; waves <= 8; ++waves) {
+        const int slices = std::min(max_slices, std::max(1, (waves * wave + iblocks / 2) / iblocks));
+        const int blocks = iblocks * slices;
+        const double eff = static_cast<double>(blocks) / (static_cast<double>((blocks + wave - 1) / wave) * wave);
+        // Prefer full waves; among equals, fewer slices (less partial-sum traffic).
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = slices;
+        }
+        if (eff > 0.97) break;
+    }
+    sh.slices = iblocks * 1 >= wave ? 1 : best;
     return sh;
 }
 
@@ -210,8 +249,8 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
                    float4* acc, float4* partial, unsigned* err, cudaStream_t s) {
     if (n <= 0) return;
     int slices = shape.slices < 1 ? 1 : shape.slices;
+    // Slices are whole 16-byte bodies of any length; tiles inside a slice may be partial.
     int jslice = (n + slices - 1) / slices;
-    jslice = (jslice + TILE - 1) / TILE * TILE;
     slices = (n + jslice - 1) / jslice;
     const bool final_out = slices == 1;
     float4* out = final_out ? acc : partial;

@@ -51,6 +51,13 @@ Engine::Engine(int device) : dev(device) {
         group_max = static_cast<int>(v);
     }
     if (walk_body) group_max = 1;
+    // Direct launch shape override "ipt,slices" (tuning; otherwise chosen per size).
+    if (const char* d = std::getenv("LETTUCE_GB300_DIRECT")) {
+        int ipt = 0, slices = 0;
+        if (std::sscanf(d, "%d,%d", &ipt, &slices) != 2 || (ipt != 1 && ipt != 2 && ipt != 4 && ipt != 8) || slices < 1)
+            fail(kRuntime, std::string("LETTUCE_GB300_DIRECT must be 'ipt,slices' with ipt in {1,2,4,8}, not '") + d + "'");
+        direct_shape_override = DirectShape{ipt, 256, slices};
+    }
     name += walk_body ? ", per-body walk" : ", group walk " + std::to_string(group_max);
     LG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& ev : events) LG_CK(cudaEventCreate(&ev));
@@ -272,7 +279,7 @@ lg_diag Engine::diagnostics() {
     lg_diag d{};
     d.has_pe = has_pe ? 1 : 0;
     if (n == 0) return d;
-    const int blocks = std::min(1024, (n + 255) / 256);
+    const int blocks = std::min(2 * sms, (n + 255) / 256);
     diag_partial.reserve(static_cast<size_t>(blocks) * 12 * 8);
     double* out = dscratch();
     launch_diag(bodies(cur), acc.as<float4>(), n, diag_partial.as<double>(), ticket(), out, blocks, stream);
@@ -315,7 +322,7 @@ void Engine::local_bounds(float lo[3], float hi[3]) {
     LG_CK(cudaSetDevice(dev));
     for (int c = 0; c < 3; ++c) lo[c] = hi[c] = 0.f;
     if (n == 0) return;
-    const int blocks = std::min(1024, (n + 255) / 256);
+    const int blocks = std::min(2 * sms, (n + 255) / 256);
     diag_partial.reserve(static_cast<size_t>(blocks) * 12 * 8);
     double* out = dscratch();
     launch_bounds(bodies(cur), n, diag_partial.as<double>(), ticket(), out, blocks, stream);

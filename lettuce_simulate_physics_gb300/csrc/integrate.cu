@@ -122,12 +122,19 @@ __global__ void k_diag(const BodyArrays b, const float4* __restrict__ acc, int n
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x < NDIAG) {
-        __threadfence();
-        double s = 0;
-        for (int blk = 0; blk < static_cast<int>(gridDim.x); ++blk) s += __ldcg(&partial[blk * NDIAG + threadIdx.x]);
-        out[threadIdx.x] = s;
-        if (threadIdx.x == 0) *ticket = 0;
+    if (!last) return;
+    // The last block sums the partials: every thread a strided subset, then the block in a fixed
+    // order, so the result does not depend on which block finished last.
+    __threadfence();
+    double t[NDIAG] = {};
+    for (int blk = threadIdx.x; blk < static_cast<int>(gridDim.x); blk += BS)
+#pragma unroll
+        for (int k = 0; k < NDIAG; ++k) t[k] += __ldcg(&partial[blk * NDIAG + k]);
+    __syncthreads();
+    block_sum(t, sh);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NDIAG; ++k) out[k] = t[k];
+        *ticket = 0;
     }
 }
 
@@ -166,15 +173,31 @@ __global__ void k_bounds(const BodyArrays b, int n, double* partial, unsigned* t
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x < 6) {
-        __threadfence();
-        const int c = threadIdx.x;
-        double r = __ldcg(&partial[c]);
-        for (int blk = 1; blk < static_cast<int>(gridDim.x); ++blk) {
-            double t = __ldcg(&partial[blk * 6 + c]);
-            r = c < 3 ? fmin(r, t) : fmax(r, t);
+    if (!last) return;
+    __threadfence();
+    double r[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int blk = threadIdx.x; blk < static_cast<int>(gridDim.x); blk += BS)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double t = __ldcg(&partial[blk * 6 + c]);
+            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
         }
-        out6[c] = r;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, r[c], o);
+            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
+        }
+    }
+    __syncthreads();
+    if (lane == 0)
+        for (int c = 0; c < 6; ++c) sh[c][w] = r[c];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int c = threadIdx.x;
+        double q = sh[c][0];
+        for (int u = 1; u < BS / 32; ++u) q = c < 3 ? fmin(q, sh[c][u]) : fmax(q, sh[c][u]);
+        out6[c] = q;
         if (c == 0) *ticket = 0;
     }
 }

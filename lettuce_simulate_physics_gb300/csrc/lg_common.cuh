@@ -139,6 +139,51 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
         : "memory");
 }
 
+// ---- PTX: packed FP32 pairs (sm_100+ f32x2 arithmetic) ----------------------------------------
+// One instruction operates on two floats held in a 64-bit register pair: the same FP32 pipe
+// throughput as scalar FFMA, at half the issue slots.
+typedef unsigned long long f2x;
+
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+    f2x d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(f2x v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
+    f2x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+    f2x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+    f2x d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2x f2_rsqrt(f2x a) {
+    float lo, hi;
+    f2_unpack(a, lo, hi);
+    return f2_pack(rsqrt_mufu(lo), rsqrt_mufu(hi));
+}
+__device__ __forceinline__ f2x f2_bcast(float v) { return f2_pack(v, v); }
+__device__ __forceinline__ float f2_sum(f2x v) {
+    float lo, hi;
+    f2_unpack(v, lo, hi);
+    return lo + hi;
+}
+
 // ---- compensated summation ---------------------------------------------------------------
 // Kahan step: adds x to (s, c), c carrying the low-order bits lost by s.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {

@@ -79,6 +79,8 @@ struct TreeState {
     DevBuf nd_range, nd_com, nd_comlo, nd_q0, nd_q1, nd_geo, nd_parent, nd_arrive;
     // groups
     DevBuf gflag, gidx, grp_node, grp_range, grp_box, leaf_cnt;
+    // upsweep order
+    DevBuf ups, dep_nodes, leaf_order;
     // scan state
     DevBuf scan_state, scan_ctr;
     size_t K = 0, T = 0, ngroups = 0, nruns = 0;
@@ -168,15 +170,30 @@ __global__ void k_frame(const BodyArrays b, int n, double* partial, unsigned* ti
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        double r[6];
-        for (int c = 0; c < 6; ++c) r[c] = __ldcg(&partial[c]);
-        for (int blk = 1; blk < static_cast<int>(gridDim.x); ++blk)
-            for (int c = 0; c < 6; ++c) {
-                double t = __ldcg(&partial[blk * 6 + c]);
-                r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
-            }
+    if (!last) return;
+    __threadfence();
+    double r[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int blk = threadIdx.x; blk < static_cast<int>(gridDim.x); blk += BS)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double t = __ldcg(&partial[blk * 6 + c]);
+            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
+        }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, r[c], o);
+            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
+        }
+    __syncthreads();
+    if (lane == 0)
+        for (int c = 0; c < 6; ++c) sh[c][w] = r[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < 6; ++c) {
+            r[c] = sh[c][0];
+            for (int u = 1; u < BS / 32; ++u) r[c] = c < 3 ? fmin(r[c], sh[c][u]) : fmax(r[c], sh[c][u]);
+        }
         // src/cpu_backend.cpp:404-406: side = max extent, widened by 1e-6; 1 if all coincide.
         double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
         side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
@@ -546,19 +563,39 @@ __global__ void k_gather_keys(const uint64_t* __restrict__ src, const uint32_t* 
 // ---- leaves ----------------------------------------------------------------------------------
 // Per body: leaf depth and group depth from window common prefixes; cap(i) = 21 inside a
 // coincident frame-0 run, 42 otherwise. bdepth packs (leaf depth, group depth) as bytes.
-__global__ void k_body_depth(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
-                             const int* __restrict__ runid, const double* __restrict__ cube, int n, int gmax,
-                             uint16_t* __restrict__ bdepth) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Each block handles DEPTH_BS bodies: it first forms, in shared memory, the common prefixes
+// c_w(j) = cpl(key j, key j+w) of every window start its bodies need (w = 16 and w = group_max),
+// then every thread takes the maxima over its windows from shared memory.
+constexpr int DEPTH_BS = 256;
+constexpr int GMAX_LIMIT = 1024;
+
+__global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+                                                         const int* __restrict__ runid, const double* __restrict__ cube,
+                                                         int n, int gmax, uint16_t* __restrict__ bdepth) {
+    __shared__ int8_t c16[DEPTH_BS + LEAF_MAX];
+    __shared__ int8_t cg[DEPTH_BS + GMAX_LIMIT];
+    const int i0 = blockIdx.x * DEPTH_BS;
+    // Window starts j in [i0 - w, i0 + DEPTH_BS): slot j - (i0 - w).
+    for (int t = threadIdx.x; t < DEPTH_BS + LEAF_MAX; t += DEPTH_BS) {
+        const int j = i0 - LEAF_MAX + t;
+        c16[t] = static_cast<int8_t>((j >= 0 && j + LEAF_MAX < n) ? cpl42(k0, k1, j, j + LEAF_MAX) : -1);
+    }
+    for (int t = threadIdx.x; t < DEPTH_BS + gmax; t += DEPTH_BS) {
+        const int j = i0 - gmax + t;
+        cg[t] = static_cast<int8_t>((j >= 0 && j + gmax < n) ? cpl42(k0, k1, j, j + gmax) : -1);
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.x;
     if (i >= n) return;
+    // Windows containing i start at j in [i - w, i], i.e. slots [threadIdx.x, threadIdx.x + w].
     int best = -1;
-    for (int j = max(0, i - LEAF_MAX); j <= i && j + LEAF_MAX < n; ++j) best = max(best, cpl42(k0, k1, j, j + LEAF_MAX));
+    for (int t = threadIdx.x; t <= threadIdx.x + LEAF_MAX; ++t) best = max(best, static_cast<int>(c16[t]));
     int cap = MAX_DEPTH;
-    if (runid && runid[i] >= 0 && cube[5 * runid[i] + 3] == 0) cap = MAX_LEVEL;
     if (!k1) cap = MAX_LEVEL;
+    else if (runid[i] >= 0 && cube[5 * runid[i] + 3] == 0) cap = MAX_LEVEL;
     const int ld = min(best + 1, cap);
     int gbest = -1;
-    for (int j = max(0, i - gmax); j <= i && j + gmax < n; ++j) gbest = max(gbest, cpl42(k0, k1, j, j + gmax));
+    for (int t = threadIdx.x; t <= threadIdx.x + gmax; ++t) gbest = max(gbest, static_cast<int>(cg[t]));
     const int gd = min(ld, gbest + 1);
     bdepth[i] = static_cast<uint16_t>(ld | (gd << 8));
 }
@@ -577,11 +614,12 @@ __global__ void k_leaf_flags(const uint64_t* __restrict__ k0, const uint64_t* __
 __global__ void k_leaf_info(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
                             const uint16_t* __restrict__ bdepth, const uint32_t* __restrict__ flag,
                             const uint32_t* __restrict__ lid, int n, uint32_t* leaf_first, uint8_t* leaf_depth,
-                            int8_t* leaf_c, uint32_t* leaf_nodes) {
+                            int8_t* leaf_c, uint32_t* leaf_nodes, int* max_depth) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !flag[i]) return;
     const uint32_t l = lid[i];
     const int d = bdepth[i] & 255;
+    atomicMax(max_depth, d);
     const int c = i == 0 ? -1 : cpl42(k0, k1, i - 1, i);
     leaf_first[l] = static_cast<uint32_t>(i);
     leaf_depth[l] = static_cast<uint8_t>(d);
@@ -800,64 +838,125 @@ __device__ void store_moments(Moments mo, uint32_t node, double M, double cx, do
 #define DMUL __dmul_rn
 #define DSUB __dsub_rn
 
-__global__ void k_upsweep(const uint32_t* __restrict__ leaf_node, uint32_t K, uint32_t T,
-                          const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo,
-                          const uint32_t* __restrict__ nd_parent, unsigned* arrive, const BodyArrays b, Moments mo,
-                          float inv_theta, unsigned* err) {
+// Upsweep bookkeeping: internal nodes bucketed by depth, leaves bucketed by body count.
+constexpr int NDEP = 48;   // depth buckets (depth <= 42)
+constexpr int NLSZ = 18;   // leaf-size buckets: 1..16, then larger
+struct UpsweepIndex {
+    unsigned dep_count[NDEP], dep_off[NDEP + 1], dep_cur[NDEP];
+    unsigned lsz_count[NLSZ], lsz_off[NLSZ + 1], lsz_cur[NLSZ];
+};
+
+__device__ __forceinline__ int lsz_bucket(uint32_t cnt) { return cnt > 16 ? 17 : static_cast<int>(cnt); }
+
+// Pass 1: bucket counts (block-aggregated). Pass 2 (phase 1): scatter into bucket order.
+__global__ void k_upsweep_bucket(const uint2* pn_lohi, const uint16_t* pn_meta, const uint32_t* pn_cpu, uint32_t T,
+                                 UpsweepIndex* ix, int phase, uint32_t* dep_nodes, uint32_t* leaf_order) {
+    __shared__ unsigned sc[NDEP + NLSZ], sbase[NDEP + NLSZ];
+    for (int k = threadIdx.x; k < NDEP + NLSZ; k += blockDim.x) sc[k] = 0;
+    __syncthreads();
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    int bucket = -1;
+    unsigned rank = 0;
+    uint32_t me = 0;
+    if (v < T) {
+        const uint16_t meta = pn_meta[v];
+        me = pn_cpu[v];
+        if (meta & 256) {
+            const uint2 r = pn_lohi[v];
+            bucket = NDEP + lsz_bucket(r.y - r.x);
+        } else {
+            bucket = meta & 255;
+        }
+        rank = atomicAdd(&sc[bucket], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < NDEP + NLSZ; k += blockDim.x) {
+        if (!sc[k]) continue;
+        if (phase == 0) {
+            atomicAdd(k < NDEP ? &ix->dep_count[k] : &ix->lsz_count[k - NDEP], sc[k]);
+        } else {
+            sbase[k] = k < NDEP ? ix->dep_off[k] + atomicAdd(&ix->dep_cur[k], sc[k])
+                                : ix->lsz_off[k - NDEP] + atomicAdd(&ix->lsz_cur[k - NDEP], sc[k]);
+        }
+    }
+    if (phase == 0) return;
+    __syncthreads();
+    if (bucket < 0) return;
+    const unsigned pos = sbase[bucket] + rank;
+    if (bucket < NDEP) dep_nodes[pos] = me;
+    else leaf_order[pos] = me;
+}
+
+__global__ void k_upsweep_offsets(UpsweepIndex* ix) {
+    if (threadIdx.x != 0) return;
+    unsigned run = 0;
+    for (int k = 0; k < NDEP; ++k) { ix->dep_off[k] = run; run += ix->dep_count[k]; }
+    ix->dep_off[NDEP] = run;
+    run = 0;
+    for (int k = 0; k < NLSZ; ++k) { ix->lsz_off[k] = run; run += ix->lsz_count[k]; }
+    ix->lsz_off[NLSZ] = run;
+}
+
+// Leaf moments about each leaf's centre of mass in FP64 (src/cpu_backend.cpp:619-640), one
+// thread per leaf, leaves taken in body-count order so a warp's loops have equal trip counts.
+__global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t K, uint32_t T,
+                               const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo, const BodyArrays b,
+                               Moments mo, float inv_theta, unsigned* err) {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= K) return;
-    uint32_t node = leaf_node[l];
+    const uint32_t node = leaf_order[l];
     if (node >= T) {
         atomicOr(err, kErrNodeOverflow);
         return;
     }
-    {
-        // Leaf moments about the leaf's centre of mass (src/cpu_backend.cpp:619-640).
-        const uint4 r = nd_range[node];
-        const float4 g = nd_geo[node];
-        double M = 0, sx = 0, sy = 0, sz = 0;
-        for (uint32_t i = r.x; i < r.y; ++i) {
-            const double m = b.m[i];
-            M = DADD(M, m);
-            sx = DADD(sx, DMUL(m, b.x[i]));
-            sy = DADD(sy, DMUL(m, b.y[i]));
-            sz = DADD(sz, DMUL(m, b.z[i]));
-        }
-        const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
-                     cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
-        double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
-        for (uint32_t i = r.x; i < r.y; ++i) {
-            const double m = b.m[i], dx = DSUB(b.x[i], cx), dy = DSUB(b.y[i], cy), dz = DSUB(b.z[i], cz);
-            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
-            qxx = DADD(qxx, DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
-            qyy = DADD(qyy, DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
-            qzz = DADD(qzz, DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
-            qxy = DADD(qxy, DMUL(DMUL(DMUL(m, 3.0), dx), dy));
-            qxz = DADD(qxz, DMUL(DMUL(DMUL(m, 3.0), dx), dz));
-            qyz = DADD(qyz, DMUL(DMUL(DMUL(m, 3.0), dy), dz));
-        }
-        store_moments(mo, node, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+    const uint4 r = nd_range[node];
+    const float4 g = nd_geo[node];
+    double M = 0, sx = 0, sy = 0, sz = 0;
+    for (uint32_t i = r.x; i < r.y; ++i) {
+        const double m = b.m[i];
+        M = DADD(M, m);
+        sx = DADD(sx, DMUL(m, b.x[i]));
+        sy = DADD(sy, DMUL(m, b.y[i]));
+        sz = DADD(sz, DMUL(m, b.z[i]));
     }
-    // Climb: the last child to arrive at a parent combines all of its children in index order.
-    // A path is at most 2*21+1 nodes long; the cap and the range checks stop a malformed tree.
-    for (int steps = 0; node != 0; ++steps) {
-        const uint32_t p = nd_parent[node];
-        if (p >= T || steps > 4 * MAX_DEPTH) {
+    const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
+                 cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
+    double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
+    for (uint32_t i = r.x; i < r.y; ++i) {
+        const double m = b.m[i], dx = DSUB(b.x[i], cx), dy = DSUB(b.y[i], cy), dz = DSUB(b.z[i], cz);
+        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+        const double m3 = DMUL(m, 3.0);
+        qxx = DADD(qxx, DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
+        qyy = DADD(qyy, DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
+        qzz = DADD(qzz, DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
+        qxy = DADD(qxy, DMUL(DMUL(m3, dx), dy));
+        qxz = DADD(qxz, DMUL(DMUL(m3, dx), dz));
+        qyz = DADD(qyz, DMUL(DMUL(m3, dy), dz));
+    }
+    store_moments(mo, node, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+}
+
+// Internal nodes of one depth: combine the children (already final) in index order, FP64, the
+// parallel-axis theorem for the traceless quadrupole (src/cpu_backend.cpp:642-663).
+__global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth, uint32_t T,
+                                const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo, Moments mo,
+                                float inv_theta, unsigned* err) {
+    const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
+    for (unsigned k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
+        const uint32_t p = dep_nodes[k];
+        if (p >= T) {
             atomicOr(err, kErrNodeOverflow);
-            return;
+            continue;
         }
         const uint4 r = nd_range[p];
         if (r.w == 0 || r.z + r.w > T) {
             atomicOr(err, kErrNodeOverflow);
-            return;
+            continue;
         }
-        __threadfence();
-        if (atomicAdd(&arrive[p], 1u) != r.w - 1) return;
-        __threadfence();
         const float4 g = nd_geo[p];
         double M = 0, sx = 0, sy = 0, sz = 0;
         for (uint32_t c = r.z; c < r.z + r.w; ++c) {
-            const float4 cm = __ldcg(&mo.com[c]);
+            const float4 cm = mo.com[c];
             const double m = cm.w;
             M = DADD(M, m);
             sx = DADD(sx, DMUL(m, static_cast<double>(cm.x)));
@@ -868,21 +967,21 @@ __global__ void k_upsweep(const uint32_t* __restrict__ leaf_node, uint32_t K, ui
                      cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
         double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
         for (uint32_t c = r.z; c < r.z + r.w; ++c) {
-            const float4 cm = __ldcg(&mo.com[c]);
-            const float4 a = __ldcg(&mo.q0[c]);
-            const float4 e = __ldcg(&mo.q1[c]);
+            const float4 cm = mo.com[c];
+            const float4 a = mo.q0[c];
+            const float4 e = mo.q1[c];
             const double m = cm.w, dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
                          dz = DSUB(static_cast<double>(cm.z), cz);
             const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+            const double m3 = DMUL(m, 3.0);
             qxx = DADD(qxx, DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2))));
             qyy = DADD(qyy, DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2))));
             qzz = DADD(qzz, DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2))));
-            qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(DMUL(m, 3.0), dx), dy)));
-            qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(DMUL(m, 3.0), dx), dz)));
-            qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(DMUL(m, 3.0), dy), dz)));
+            qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy)));
+            qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz)));
+            qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz)));
         }
         store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
-        node = p;
     }
 }
 
@@ -972,7 +1071,7 @@ void tree_sort(Engine& e) {
     t.counts.reserve(64);
     t.restarted = false;
     t.nruns = 0;
-    const int fb = std::min(1024, grid_for(n, BS));
+    const int fb = std::min(2 * e.sms, grid_for(n, BS));
     e.diag_partial.reserve(static_cast<size_t>(fb) * 12 * 8);
     k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<double>(), e.ticket(), t.frame.as<double>());
     LG_LAUNCHED();
@@ -1057,7 +1156,8 @@ void tree_build(Engine& e, double theta) {
     t.leaf_pre.reserve(n1 * 4);
     t.leaf_node.reserve(n1 * 4);
     const int gb = grid_for(n, BS);
-    k_body_depth<<<gb, BS, 0, s>>>(k0, k1, runid, cube, n, t.group_max, t.bdepth.as<uint16_t>());
+    if (t.group_max > GMAX_LIMIT) fail(kRuntime, "cuda tree build: group size above 1024");
+    k_body_depth<<<grid_for(n, DEPTH_BS), DEPTH_BS, 0, s>>>(k0, k1, runid, cube, n, t.group_max, t.bdepth.as<uint16_t>());
     LG_LAUNCHED();
     k_leaf_flags<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
     LG_LAUNCHED();
@@ -1066,7 +1166,7 @@ void tree_build(Engine& e, double theta) {
     LG_CK(cudaMemsetAsync(t.leaf_cnt.as<char>(), 0, n1 * 4, s));
     k_leaf_info<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
                                   t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
-                                  t.leaf_cnt.as<uint32_t>());
+                                  t.leaf_cnt.as<uint32_t>(), reinterpret_cast<int*>(counts + 4));
     LG_LAUNCHED();
     k_lid<<<gb, BS, 0, s>>>(t.leafid.as<uint32_t>(), t.flag.as<uint32_t>(), n);
     LG_LAUNCHED();
@@ -1074,10 +1174,11 @@ void tree_build(Engine& e, double theta) {
     LG_LAUNCHED();
     e.launches += 3;
     scan_u32(e, t, t.leaf_cnt.as<uint32_t>(), t.leaf_pre.as<uint32_t>(), n + 1, counts + 2);
-    LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 16, cudaMemcpyDeviceToHost, s));
+    LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 32, cudaMemcpyDeviceToHost, s));
     LG_CK(cudaStreamSynchronize(s));
     t.K = e.pinned_small[1];
     t.T = e.pinned_small[2];
+    t.max_depth = static_cast<int>(e.pinned_small[4]);
     const size_t K = t.K, T = t.T;
     if (K < 1 || K > static_cast<size_t>(n) || T < K)
         fail(kRuntime, "cuda tree build: bad leaf/node count " + std::to_string(K) + "/" + std::to_string(T));
@@ -1129,15 +1230,35 @@ void tree_build(Engine& e, double theta) {
                                e.bodies(e.cur), counts + 3,
                                t.grp_range.as<uint2>(), t.grp_box.as<float4>());
     LG_LAUNCHED();
-    LG_CK(cudaMemsetAsync(t.nd_arrive.as<char>(), 0, T * 4, s));
+    // Upsweep: leaves (by size), then internal nodes level by level from the deepest.
+    t.ups.reserve(sizeof(UpsweepIndex));
+    t.dep_nodes.reserve(T * 4);
+    t.leaf_order.reserve(K * 4);
+    UpsweepIndex* ix = t.ups.as<UpsweepIndex>();
+    LG_CK(cudaMemsetAsync(ix, 0, sizeof(UpsweepIndex), s));
+    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(),
+                                       static_cast<uint32_t>(T), ix, 0, nullptr, nullptr);
+    LG_LAUNCHED();
+    k_upsweep_offsets<<<1, 32, 0, s>>>(ix);
+    LG_LAUNCHED();
+    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(),
+                                       static_cast<uint32_t>(T), ix, 1, t.dep_nodes.as<uint32_t>(),
+                                       t.leaf_order.as<uint32_t>());
+    LG_LAUNCHED();
     const float inv_theta = theta > 0 ? static_cast<float>(1.0 / theta) : FLT_MAX;
     Moments mo{t.nd_com.as<float4>(), t.nd_comlo.as<float4>(), t.nd_q0.as<float4>(), t.nd_q1.as<float4>()};
-    k_upsweep<<<grid_for(static_cast<long long>(K), 128), 128, 0, s>>>(
-        t.leaf_node.as<uint32_t>(), static_cast<uint32_t>(K), static_cast<uint32_t>(T), t.nd_range.as<uint4>(),
-        t.nd_geo.as<float4>(), t.nd_parent.as<uint32_t>(), t.nd_arrive.as<unsigned>(), e.bodies(e.cur), mo,
-        inv_theta, e.err_word());
+    k_leaf_moments<<<grid_for(static_cast<long long>(K), 128), 128, 0, s>>>(
+        t.leaf_order.as<uint32_t>(), static_cast<uint32_t>(K), static_cast<uint32_t>(T), t.nd_range.as<uint4>(),
+        t.nd_geo.as<float4>(), e.bodies(e.cur), mo, inv_theta, e.err_word());
     LG_LAUNCHED();
-    e.launches += 4;
+    e.launches += 6;
+    const int cb = std::max(1, std::min(4 * e.sms, grid_for(static_cast<long long>(T), 128)));
+    for (int d = t.max_depth - 1; d >= 0; --d) {
+        k_combine_level<<<cb, 128, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, static_cast<uint32_t>(T),
+                                           t.nd_range.as<uint4>(), t.nd_geo.as<float4>(), mo, inv_theta, e.err_word());
+        LG_LAUNCHED();
+        ++e.launches;
+    }
 }
 
 TreeView tree_view(Engine& e) {
@@ -1248,7 +1369,7 @@ size_t tree_held_bytes(const Engine& e) {
                             &t.runid, &t.bdepth, &t.flag, &t.leafid, &t.frame, &t.runs, &t.runcube, &t.counts,
                             &t.leaf_first, &t.leaf_depth, &t.leaf_c, &t.leaf_pre, &t.leaf_node, &t.pn_lohi,
                             &t.pn_meta, &t.pn_nchild, &t.pn_cb, &t.pn_cpu, &t.nd_range, &t.nd_com, &t.nd_comlo,
-                            &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.nd_arrive, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt,
+                            &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.nd_arrive, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt, &t.ups, &t.dep_nodes, &t.leaf_order,
                             &t.grp_range, &t.grp_box, &t.scan_state, &t.scan_ctr})
         h += d->capacity();
     return h;

@@ -9,10 +9,13 @@
 //    bodies, opened internal nodes push their children. Appends are warp-compacted with ballots.
 //    The traversal stack lives in global memory (one slice per warp).
 //  - Evaluation in chunks: when the lists fill up, the warp converts the entries once to
-//    coordinates relative to the group's box centre o, (x_hi - o) + x_lo in FP32, in shared
-//    memory, and every lane evaluates them for its IPT i-bodies (IPT = ceil(group size / 32)):
-//    quadrupole cell terms (cuda_backend.cu:783-800 / cpu_backend.cpp:858-871 math) and
-//    softened body terms. Chunk sums are added to the running sums with Kahan compensation.
+//    coordinates relative to the group's box centre o, (x_hi - o) + x_lo in FP32, into
+//    struct-of-arrays chunks in shared memory, and every lane evaluates them for its IPT i-bodies
+//    (IPT = ceil(group size / 32)): quadrupole cell terms (cuda_backend.cu:783-800 /
+//    cpu_backend.cpp:858-871 math) and softened body terms. Two consecutive entries are loaded
+//    as one float2 and evaluated together with packed f32x2 instructions (one issue slot for two
+//    FP32 operations). Chunk sums are added to running sums kept in shared memory with Kahan
+//    compensation.
 // The interaction count per body is the list length minus its own entry; the reference CPU
 // backend counts that self entry, so its count exceeds this one by exactly N.
 #include "engine.cuh"
@@ -22,6 +25,9 @@ namespace lg {
 namespace {
 
 constexpr int WBS = 128;  // 4 warps per block
+#ifndef LG_WALK_MINB
+#define LG_WALK_MINB 4  // resident blocks per SM the register budget is sized for
+#endif
 constexpr int WARPS = WBS / 32;
 constexpr int SMALL_LEAF = 4;   // src/cpu_backend.cpp:29
 constexpr int SCAP = 16384;     // traversal stack entries per warp (global memory)
@@ -32,14 +38,16 @@ constexpr int CCH = 64;   // cells converted per chunk
 constexpr int BCH = 128;  // bodies converted per chunk
 constexpr int PASS = 128; // i-bodies per pass (4 per lane)
 
-struct WarpSmem {
+constexpr int IPT_MAX = 4;
+
+// Per-warp shared memory. Chunks are struct-of-arrays so that entries k, k+1 load as one float2.
+struct __align__(16) WarpSmem {
+    float cx[CCH], cy[CCH], cz[CCH], cm[CCH], qxx[CCH], qxy[CCH], qxz[CCH], qyy[CCH], qyz[CCH], qzz[CCH];
+    float bx[BCH], by[BCH], bz[BCH], bm[BCH];
+    float ks[IPT_MAX][8][32];  // Kahan sums sx sy sz sp and compensations cx cy cz cp, per slot and lane
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];
     uint32_t rpre[RL_CAP + 1];
-    float4 cpos[CCH];
-    float4 cq0[CCH];
-    float2 cq1[CCH];
-    float4 bpos[BCH];
 };
 
 struct WalkArgs {
@@ -66,98 +74,161 @@ __device__ __forceinline__ int warp_excl_scan(int v, int lane, int& total) {
     return x - v;
 }
 
+__device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
+
+// Adds one chunk's partial sums (packed halves) of slot u into the lane's Kahan sums.
+template <bool POT>
+__device__ __forceinline__ void merge_slot(WarpSmem& s, int u, int lane, f2x ax, f2x ay, f2x az, f2x ap) {
+    float* k = &s.ks[u][0][lane];
+    float sx = k[0], sy = k[32], sz = k[64], cx = k[128], cy = k[160], cz = k[192];
+    kahan_add(sx, cx, f2_sum(ax));
+    kahan_add(sy, cy, f2_sum(ay));
+    kahan_add(sz, cz, f2_sum(az));
+    k[0] = sx; k[32] = sy; k[64] = sz; k[128] = cx; k[160] = cy; k[192] = cz;
+    if (POT) {
+        float sp = k[96], cp = k[224];
+        kahan_add(sp, cp, f2_sum(ap));
+        k[96] = sp; k[224] = cp;
+    }
+}
+
+template <bool EPS0>
+__device__ __forceinline__ f2x pair_rsqrt(f2x r2) {
+    float lo, hi;
+    f2_unpack(r2, lo, hi);
+    float a = rsqrt_mufu(lo), b = rsqrt_mufu(hi);
+    if (EPS0) {
+        a = lo > 0.f ? a : 0.f;
+        b = hi > 0.f ? b : 0.f;
+    }
+    return f2_pack(a, b);
+}
+
+// Quadrupole cell terms: d points from the body to the cell,
+// a = G [M d/r^3 - Q d/r^5 + 5/2 (dQd) d/r^7], phi = -G [M/r + 1/2 dQd/r^5]. cc is even.
 template <int IPT, bool POT, bool EPS0>
-struct Acc {
-    float sx[IPT], sy[IPT], sz[IPT], sp[IPT], cx[IPT], cy[IPT], cz[IPT], cp[IPT];
-    float px[IPT], py[IPT], pz[IPT], pp[IPT];
-    __device__ void zero_all() {
+__device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int lane, const float (&xi)[IPT_MAX],
+                                           const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+    f2x XI[IPT], YI[IPT], ZI[IPT], ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
-        for (int u = 0; u < IPT; ++u) sx[u] = sy[u] = sz[u] = sp[u] = cx[u] = cy[u] = cz[u] = cp[u] = 0.f;
+    for (int u = 0; u < IPT; ++u) {
+        XI[u] = f2_bcast(xi[u]);
+        YI[u] = f2_bcast(yi[u]);
+        ZI[u] = f2_bcast(zi[u]);
+        ax[u] = ay[u] = az[u] = ap[u] = 0ull;
     }
-    __device__ void zero_partial() {
-#pragma unroll
-        for (int u = 0; u < IPT; ++u) px[u] = py[u] = pz[u] = pp[u] = 0.f;
-    }
-    __device__ void merge() {
+    const f2x E2 = f2_bcast(e2), C25 = f2_bcast(2.5f), NEG1 = f2_bcast(-1.f), C05 = f2_bcast(0.5f);
+    // Few i-bodies per lane leave little independent work per entry: unroll over entries then.
+#pragma unroll 1
+    for (int k = 0; k < cc; k += 2) {
+        const f2x X = ld2(s.cx + k), Y = ld2(s.cy + k), Z = ld2(s.cz + k), M = ld2(s.cm + k);
+        const f2x QXX = ld2(s.qxx + k), QXY = ld2(s.qxy + k), QXZ = ld2(s.qxz + k);
+        const f2x QYY = ld2(s.qyy + k), QYZ = ld2(s.qyz + k), QZZ = ld2(s.qzz + k);
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-            kahan_add(sx[u], cx[u], px[u]);
-            kahan_add(sy[u], cy[u], py[u]);
-            kahan_add(sz[u], cz[u], pz[u]);
-            if (POT) kahan_add(sp[u], cp[u], pp[u]);
+            const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+            const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+            const f2x inv = pair_rsqrt<EPS0>(r2);
+            const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv, inv2), inv5 = f2_mul(inv3, inv2);
+            const f2x qx = f2_fma(QXX, dx, f2_fma(QXY, dy, f2_mul(QXZ, dz)));
+            const f2x qy = f2_fma(QXY, dx, f2_fma(QYY, dy, f2_mul(QYZ, dz)));
+            const f2x qz = f2_fma(QXZ, dx, f2_fma(QYZ, dy, f2_mul(QZZ, dz)));
+            const f2x dqd = f2_fma(dx, qx, f2_fma(dy, qy, f2_mul(dz, qz)));
+            const f2x t5 = f2_mul(dqd, inv5);
+            const f2x f = f2_fma(M, inv3, f2_mul(f2_mul(C25, t5), inv2));
+            const f2x n5 = f2_mul(inv5, NEG1);
+            ax[u] = f2_fma(qx, n5, f2_fma(f, dx, ax[u]));
+            ay[u] = f2_fma(qy, n5, f2_fma(f, dy, ay[u]));
+            az[u] = f2_fma(qz, n5, f2_fma(f, dz, az[u]));
+            if (POT) ap[u] = f2_add(ap[u], f2_fma(M, inv, f2_mul(C05, t5)));
         }
     }
-};
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) merge_slot<POT>(s, u, lane, ax[u], ay[u], az[u], ap[u]);
+}
 
+// Softened body terms a = G m d / r^3, phi = -G m / r. bc is even.
 template <int IPT, bool POT, bool EPS0>
-__device__ __forceinline__ void eval_cells(const WarpSmem& s, int cc, const float (&xi)[IPT], const float (&yi)[IPT],
-                                           const float (&zi)[IPT], float e2, Acc<IPT, POT, EPS0>& a) {
+__device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int lane, const float (&xi)[IPT_MAX],
+                                            const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+    f2x XI[IPT], YI[IPT], ZI[IPT], ax[IPT], ay[IPT], az[IPT], ap[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) {
+        XI[u] = f2_bcast(xi[u]);
+        YI[u] = f2_bcast(yi[u]);
+        ZI[u] = f2_bcast(zi[u]);
+        ax[u] = ay[u] = az[u] = ap[u] = 0ull;
+    }
+    const f2x E2 = f2_bcast(e2);
 #pragma unroll 2
-    for (int k = 0; k < cc; ++k) {
-        const float4 p = s.cpos[k];
-        const float4 q0 = s.cq0[k];
-        const float2 q1 = s.cq1[k];
+    for (int k = 0; k < bc; k += 2) {
+        const f2x X = ld2(s.bx + k), Y = ld2(s.by + k), Z = ld2(s.bz + k), M = ld2(s.bm + k);
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
-            const float dx = p.x - xi[u], dy = p.y - yi[u], dz = p.z - zi[u];
-            const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
-            float inv = rsqrt_mufu(r2);
-            if (EPS0) inv = r2 > 0.f ? inv : 0.f;
-            const float inv2 = inv * inv, inv3 = inv * inv2, inv5 = inv3 * inv2;
-            // d points from the body to the cell: a = G [M d/r^3 - Q d/r^5 + 5/2 (dQd) d/r^7].
-            const float qx = __fmaf_rn(q0.x, dx, __fmaf_rn(q0.y, dy, q0.z * dz));
-            const float qy = __fmaf_rn(q0.y, dx, __fmaf_rn(q0.w, dy, q1.x * dz));
-            const float qz = __fmaf_rn(q0.z, dx, __fmaf_rn(q1.x, dy, q1.y * dz));
-            const float dqd = __fmaf_rn(dx, qx, __fmaf_rn(dy, qy, dz * qz));
-            const float t5 = dqd * inv5;
-            const float f = __fmaf_rn(p.w, inv3, 2.5f * t5 * inv2);
-            a.px[u] = __fmaf_rn(-qx, inv5, __fmaf_rn(f, dx, a.px[u]));
-            a.py[u] = __fmaf_rn(-qy, inv5, __fmaf_rn(f, dy, a.py[u]));
-            a.pz[u] = __fmaf_rn(-qz, inv5, __fmaf_rn(f, dz, a.pz[u]));
-            if (POT) a.pp[u] += __fmaf_rn(p.w, inv, 0.5f * t5);
+            const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+            const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+            const f2x inv = pair_rsqrt<EPS0>(r2);
+            const f2x mi = f2_mul(M, inv);  // rounded: the self term cancels exactly
+            const f2x f = f2_mul(mi, f2_mul(inv, inv));
+            ax[u] = f2_fma(f, dx, ax[u]);
+            ay[u] = f2_fma(f, dy, ay[u]);
+            az[u] = f2_fma(f, dz, az[u]);
+            if (POT) ap[u] = f2_add(ap[u], mi);
         }
+    }
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) merge_slot<POT>(s, u, lane, ax[u], ay[u], az[u], ap[u]);
+}
+
+template <bool POT, bool EPS0>
+__device__ __forceinline__ void eval_cells_n(int ipt, WarpSmem& s, int cc, int lane, const float (&xi)[IPT_MAX],
+                                             const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+    switch (ipt) {
+        case 1: eval_cells<1, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
+        case 2: eval_cells<2, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
+        case 3: eval_cells<3, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
+        default: eval_cells<4, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
     }
 }
 
-template <int IPT, bool POT, bool EPS0>
-__device__ __forceinline__ void eval_bodies(const WarpSmem& s, int bc, const float (&xi)[IPT], const float (&yi)[IPT],
-                                            const float (&zi)[IPT], float e2, Acc<IPT, POT, EPS0>& a) {
-#pragma unroll 4
-    for (int k = 0; k < bc; ++k) {
-        const float4 q = s.bpos[k];
-#pragma unroll
-        for (int u = 0; u < IPT; ++u) {
-            const float dx = q.x - xi[u], dy = q.y - yi[u], dz = q.z - zi[u];
-            const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmaf_rn(dz, dz, e2)));
-            float inv = rsqrt_mufu(r2);
-            if (EPS0) inv = r2 > 0.f ? inv : 0.f;
-            const float mi = __fmul_rn(q.w, inv);  // rounded: the self term cancels exactly
-            const float f = mi * (inv * inv);
-            a.px[u] = __fmaf_rn(f, dx, a.px[u]);
-            a.py[u] = __fmaf_rn(f, dy, a.py[u]);
-            a.pz[u] = __fmaf_rn(f, dz, a.pz[u]);
-            if (POT) a.pp[u] += mi;
-        }
+template <bool POT, bool EPS0>
+__device__ __forceinline__ void eval_bodies_n(int ipt, WarpSmem& s, int bc, int lane, const float (&xi)[IPT_MAX],
+                                              const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+    switch (ipt) {
+        case 1: eval_bodies<1, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
+        case 2: eval_bodies<2, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
+        case 3: eval_bodies<3, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
+        default: eval_bodies<4, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
     }
 }
+
+// A far, massless entry: pads a chunk to an even count and contributes exactly zero.
+constexpr float kFar = 1e18f;
 
 // Evaluates the pending lists for the pass's i-bodies and empties them.
-template <int IPT, bool POT, bool EPS0>
-__device__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int nc, int nr, float ox, float oy, float oz,
-                      const float (&xi)[IPT], const float (&yi)[IPT], const float (&zi)[IPT], Acc<IPT, POT, EPS0>& a) {
+template <bool POT, bool EPS0>
+__device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int ipt, int nc, int nr, float ox,
+                                      float oy, float oz, const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
+                                      const float (&zi)[IPT_MAX]) {
     for (int c0 = 0; c0 < nc; c0 += CCH) {
         const int cc = min(CCH, nc - c0);
-        for (int k = lane; k < cc; k += 32) {
-            const uint32_t nd = s.clist[c0 + k];
-            const float4 com = w.tv.nd_com[nd], cl = w.tv.nd_comlo[nd], q0 = w.tv.nd_q0[nd], q1 = w.tv.nd_q1[nd];
-            s.cpos[k] = make_float4((com.x - ox) + cl.x, (com.y - oy) + cl.y, (com.z - oz) + cl.z, com.w);
-            s.cq0[k] = q0;
-            s.cq1[k] = make_float2(q1.x, q1.y);
+        const int cc2 = (cc + 1) & ~1;
+        for (int k = lane; k < cc2; k += 32) {
+            if (k < cc) {
+                const uint32_t nd = s.clist[c0 + k];
+                const float4 com = w.tv.nd_com[nd], cl = w.tv.nd_comlo[nd], q0 = w.tv.nd_q0[nd], q1 = w.tv.nd_q1[nd];
+                s.cx[k] = (com.x - ox) + cl.x;
+                s.cy[k] = (com.y - oy) + cl.y;
+                s.cz[k] = (com.z - oz) + cl.z;
+                s.cm[k] = com.w;
+                s.qxx[k] = q0.x; s.qxy[k] = q0.y; s.qxz[k] = q0.z; s.qyy[k] = q0.w; s.qyz[k] = q1.x; s.qzz[k] = q1.y;
+            } else {
+                s.cx[k] = kFar; s.cy[k] = kFar; s.cz[k] = kFar; s.cm[k] = 0.f;
+                s.qxx[k] = s.qxy[k] = s.qxz[k] = s.qyy[k] = s.qyz[k] = s.qzz[k] = 0.f;
+            }
         }
         __syncwarp();
-        a.zero_partial();
-        eval_cells<IPT, POT, EPS0>(s, cc, xi, yi, zi, w.e2, a);
-        a.merge();
+        eval_cells_n<POT, EPS0>(ipt, s, cc2, lane, xi, yi, zi, w.e2);
         __syncwarp();
     }
     if (nr == 0) return;
@@ -176,33 +247,40 @@ __device__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int nc, int nr, 
     const int total = static_cast<int>(s.rpre[nr]);
     for (int b0 = 0; b0 < total; b0 += BCH) {
         const int bc = min(BCH, total - b0);
-        for (int k = lane; k < bc; k += 32) {
-            const uint32_t p = b0 + k;
-            int lo = 0, hi = nr;  // last r with rpre[r] <= p
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (s.rpre[mid] <= p) lo = mid;
-                else hi = mid;
+        const int bc2 = (bc + 1) & ~1;
+        for (int k = lane; k < bc2; k += 32) {
+            if (k < bc) {
+                const uint32_t p = b0 + k;
+                int lo = 0, hi = nr;  // last r with rpre[r] <= p
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s.rpre[mid] <= p) lo = mid;
+                    else hi = mid;
+                }
+                const uint32_t j = s.rlist[lo].x + (p - s.rpre[lo]);
+                const float4 h = w.hm[j], l = w.lo[j];
+                s.bx[k] = (h.x - ox) + l.x;
+                s.by[k] = (h.y - oy) + l.y;
+                s.bz[k] = (h.z - oz) + l.z;
+                s.bm[k] = h.w;
+            } else {
+                s.bx[k] = kFar; s.by[k] = kFar; s.bz[k] = kFar; s.bm[k] = 0.f;
             }
-            const uint32_t j = s.rlist[lo].x + (p - s.rpre[lo]);
-            const float4 h = w.hm[j], l = w.lo[j];
-            s.bpos[k] = make_float4((h.x - ox) + l.x, (h.y - oy) + l.y, (h.z - oz) + l.z, h.w);
         }
         __syncwarp();
-        a.zero_partial();
-        eval_bodies<IPT, POT, EPS0>(s, bc, xi, yi, zi, w.e2, a);
-        a.merge();
+        eval_bodies_n<POT, EPS0>(ipt, s, bc2, lane, xi, yi, zi, w.e2);
         __syncwarp();
     }
 }
 
-template <int IPT, bool POT, bool EPS0>
+template <bool POT, bool EPS0>
 __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int lane, uint2 gr, float4 bc, float4 bh,
                           uint32_t plo, int np, unsigned long long& inter_b, unsigned long long& inter_c) {
     const float ox = bc.x, oy = bc.y, oz = bc.z;
-    float xi[IPT], yi[IPT], zi[IPT], mi[IPT];
+    const int ipt = (np + 31) >> 5;
+    float xi[IPT_MAX], yi[IPT_MAX], zi[IPT_MAX], mi[IPT_MAX];
 #pragma unroll
-    for (int u = 0; u < IPT; ++u) {
+    for (int u = 0; u < IPT_MAX; ++u) {
         const int k = min(lane + 32 * u, np - 1);
         const float4 h = w.hm[plo + k], l = w.lo[plo + k];
         xi[u] = (h.x - ox) + l.x;
@@ -210,8 +288,10 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         zi[u] = (h.z - oz) + l.z;
         mi[u] = h.w;
     }
-    Acc<IPT, POT, EPS0> a;
-    a.zero_all();
+#pragma unroll
+    for (int u = 0; u < IPT_MAX; ++u)
+#pragma unroll
+        for (int f = 0; f < 8; ++f) s.ks[u][f][lane] = 0.f;
     const unsigned lt = (1u << lane) - 1u;
     int sp = 1;
     if (lane == 0) stack[0] = 0;
@@ -222,7 +302,16 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     // Each node is visited at most once per pass; the cap stops a malformed tree.
     const uint32_t max_iter = static_cast<uint32_t>(w.tv.T) + 64u;
     uint32_t iter = 0;
-    while (sp > 0) {
+    for (;;) {
+        const bool done = sp == 0;
+        // One evaluation site: when the lists fill up, and once at the end.
+        if (done || nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
+            flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi);
+            list_len += nc + nbr;
+            cells_len += nc;
+            nc = nr = nbr = 0;
+            if (done) break;
+        }
         if (++iter > max_iter) {
             overflow = true;
             break;
@@ -275,31 +364,20 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
             for (uint32_t k = 0; k < a1; ++k) stack[sp + coff + k] = a0 + (a1 - 1 - k);  // first child on top
         sp += ctot;
         __syncwarp();
-        if (nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
-            flush<IPT, POT, EPS0>(w, s, lane, nc, nr, ox, oy, oz, xi, yi, zi, a);
-            list_len += nc + nbr;
-            cells_len += nc;
-            nc = nr = nbr = 0;
-        }
     }
-    if (overflow) {
-        if (lane == 0) atomicOr(w.err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
-    } else {
-        flush<IPT, POT, EPS0>(w, s, lane, nc, nr, ox, oy, oz, xi, yi, zi, a);
-        list_len += nc + nbr;
-        cells_len += nc;
-    }
+    if (overflow && lane == 0) atomicOr(w.err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
     const float self_inv = (POT && !EPS0) ? rsqrt_mufu(w.e2) : 0.f;
 #pragma unroll
-    for (int u = 0; u < IPT; ++u) {
+    for (int u = 0; u < IPT_MAX; ++u) {
         const int k = lane + 32 * u;
         if (k >= np) continue;
         const uint32_t i = plo + k;
-        float p = a.sp[u] - a.cp[u];
+        const float* ks = &s.ks[u][0][lane];
+        float p = ks[96] - ks[224];
         // The own body is always in the list (its leaf is inside the group, so it is opened);
         // with eps > 0 its pair has d = 0 and only adds m_i/eps to the potential.
         if (POT && !EPS0) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
-        w.acc[i] = make_float4(w.G * (a.sx[u] - a.cx[u]), w.G * (a.sy[u] - a.cy[u]), w.G * (a.sz[u] - a.cz[u]),
+        w.acc[i] = make_float4(w.G * (ks[0] - ks[128]), w.G * (ks[32] - ks[160]), w.G * (ks[64] - ks[192]),
                                POT ? -w.G * p : 0.f);
         w.cost[i] = static_cast<float>(list_len - 1);
     }
@@ -308,7 +386,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
 }
 
 template <bool POT, bool EPS0>
-__global__ void __launch_bounds__(WBS) k_walk(WalkArgs w) {
+__global__ void __launch_bounds__(WBS, LG_WALK_MINB) k_walk(WalkArgs w) {
     __shared__ WarpSmem sm[WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     WarpSmem& s = sm[wid];
@@ -324,12 +402,7 @@ __global__ void __launch_bounds__(WBS) k_walk(WalkArgs w) {
         const float4 bc = w.tv.grp_box[2 * g], bh = w.tv.grp_box[2 * g + 1];
         for (uint32_t plo = gr.x; plo < gr.y; plo += PASS) {
             const int np = static_cast<int>(min(static_cast<uint32_t>(PASS), gr.y - plo));
-            switch ((np + 31) >> 5) {
-                case 1: walk_pass<1, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
-                case 2: walk_pass<2, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
-                case 3: walk_pass<3, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
-                default: walk_pass<4, POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c); break;
-            }
+            walk_pass<POT, EPS0>(w, s, stack, lane, gr, bc, bh, plo, np, inter_b, inter_c);
         }
     }
     if (lane == 0) {
