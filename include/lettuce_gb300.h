@@ -163,6 +163,19 @@ lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops);
 lg_status lg_host_alloc(size_t bytes, void** out);
 lg_status lg_host_free(void* p);
 
+/* ---- Adjoint of the leapfrog (no counterpart in the reference) -------------------------------
+ * Reverse-mode derivative of the loss L = sum_i m_i |x_i(T) - x*_i|^2 after `steps` KDK steps of
+ * size dt from the resident state, with direct-summation forces. lg_adjoint_forward runs the steps
+ * (the final state stays resident, as after ordinary steps) and keeps FP64-position / FP32-velocity
+ * checkpoints every `checkpoint_every` steps. lg_adjoint_backward takes x* (FP64, indexed by body
+ * id; ids must be 0..n-1) and returns L and dL/dx0, dL/dv0, dL/dm (FP64, indexed by id); it
+ * recomputes each segment from its checkpoint and applies one pairwise vector-Jacobian product per
+ * step. Afterwards the resident state is no longer the final state (upload again to continue). */
+lg_status lg_adjoint_forward(lg_engine* e, const lg_force_params* p, double dt, int steps, int checkpoint_every);
+lg_status lg_adjoint_backward(lg_engine* e, const double* target_x, const double* target_y, const double* target_z,
+                              double* loss, double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz,
+                              double* gm);
+
 /* Direct-summation forces with no device allocation. No counterpart in the reference: it is for
  * callers that cannot allocate device memory when they need forces, such as a code that owns all
  * device memory through its own fixed arena, or a stepping loop that must avoid cudaMalloc's

@@ -165,6 +165,8 @@ def _lib() -> C.CDLL:
         "lg_interaction_split": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "lg_probe_fp32_peak": (st, [vp, C.POINTER(C.c_double)]),
         "lg_host_alloc": (st, [C.c_size_t, C.POINTER(vp)]),
+        "lg_adjoint_forward": (st, [vp, C.POINTER(_CForceParams), C.c_double, C.c_int, C.c_int]),
+        "lg_adjoint_backward": (st, [vp, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d]),
         "lg_host_free": (st, [vp]),
     }
     for name, (res, args) in sigs.items():
@@ -386,6 +388,23 @@ class CudaBackend:
         t = C.c_double()
         _check(self._lib.lg_probe_fp32_peak(self._h, C.byref(t)))
         return float(t.value)
+
+    def adjoint_forward(self, p: ForceParams, dt: float, steps: int, checkpoint_every: int) -> None:
+        """Runs `steps` KDK steps from the resident state, keeping adjoint checkpoints."""
+        cp = _cparams(p)
+        _check(self._lib.lg_adjoint_forward(self._h, C.byref(cp), float(dt), int(steps), int(checkpoint_every)))
+
+    def adjoint_backward(self, target):
+        """Loss sum m |x(T) - target|^2 and its gradients with respect to the initial positions,
+        velocities and masses, all indexed by body id: (loss, gx (n,3), gv (n,3), gm (n,))."""
+        n = self.size()
+        t = np.ascontiguousarray(np.asarray(target, np.float64).reshape(n, 3).T)
+        out = np.zeros((7, n), np.float64)
+        loss = C.c_double()
+        ptr = [out[k].ctypes.data_as(_d) for k in range(7)]
+        _check(self._lib.lg_adjoint_backward(self._h, t[0].ctypes.data_as(_d), t[1].ctypes.data_as(_d),
+                                             t[2].ctypes.data_as(_d), C.byref(loss), *ptr))
+        return float(loss.value), out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
 
     def launch_count(self) -> int:
         c = C.c_uint64()

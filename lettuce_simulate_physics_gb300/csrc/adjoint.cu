@@ -1,0 +1,394 @@
+// Adjoint (reverse mode) of the kick-drift-kick leapfrog with direct-summation forces. The
+// reference has no adjoint; this is the engine's own, checked against FP64 central finite
+// differences and the FP64 CPU adjoint in oracle/lettuce_oracle.c.
+//
+// Forward map (the reference's step order, src/simulation.cpp:416-419): forces at x0, then per step
+// kick(dt/2), drift(dt), forces, kick(dt/2). Loss L = sum_i m_i |x_i(T) - x*_i|^2.
+//
+// Reverse sweep. With h = dt/2 the adjoint of one step is
+//   lv_h = lv';  lx' += J(x')^T (h lv');  lx = lx';  lv_h += dt lx';  lv = lv_h;  lx += J(x)^T (h lv_h)
+// and the two products at a shared position x_s (closing kick of step s-1, opening kick of step s)
+// carry the same vector, so the sweep needs one vector-Jacobian product per step:
+//   lx = dL/dx_T, lv = 0, lm = |x_T - x*|^2;  for s = T-1 .. 0:  lv += dt lx;
+//   (lx, lm) += VJP at x_s with weight c lv, c = dt (s > 0) or h (s = 0).
+// The closing-kick product at x_T carries lv_T = 0 and drops out.
+//
+// Pairwise VJP. a_k = G sum_j m_j K(d_kj), K(d) = d / s^3, s^2 = |d|^2 + eps^2, d_kj = x_j - x_k:
+//   dL/dx_k += G sum_j M(d_kj) (m_k w_j - m_j w_k),  M(d) u = u / s^3 - 3 d (d . u) / s^5
+//   dL/dm_k -= G sum_j (w_j . d_kj) / s^3
+// The self pair contributes exactly zero (d = 0, u = 0). Pair arithmetic is FP32 on block-relative
+// coordinates from the FP64 hi/lo split, packed f32x2; sums across tiles are Kahan-compensated and
+// the adjoint state is accumulated in FP64.
+//
+// Checkpoints: FP64 positions and FP32 velocities every k steps; the backward pass restores each
+// segment, recomputes its positions with the same deterministic kernels (so they are bit-identical
+// to the forward pass), and stores them as hi/lo float4 pairs for the VJP.
+#include <algorithm>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace lg {
+
+namespace {
+
+constexpr int VBS = 256;
+constexpr int VTILE = 256;
+constexpr int VIPT = 2;
+
+struct __align__(16) VjpSmem {
+    float rx[VTILE], ry[VTILE], rz[VTILE], rm[VTILE], wx[VTILE], wy[VTILE], wz[VTILE];
+};
+
+inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
+
+__device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
+
+// partial[slice][i] = (gx, gy, gz, h) for the i-bodies of this block and the j of this slice.
+template <bool EPS0>
+__global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, const float4* __restrict__ lo,
+                                             const float4* __restrict__ wv, int n, int jslice, float e2,
+                                             float4* __restrict__ partial) {
+    __shared__ VjpSmem sm;
+    const int tid = threadIdx.x;
+    const int base = blockIdx.x * (VBS * VIPT);
+    const int j0 = blockIdx.y * jslice;
+    const int j1 = min(n, j0 + jslice);
+    const float4 oh = hm[base], ol = lo[base];
+    float xi[VIPT], yi[VIPT], zi[VIPT], mk[VIPT], wkx[VIPT], wky[VIPT], wkz[VIPT];
+    float s[VIPT][4], c[VIPT][4];
+#pragma unroll
+    for (int u = 0; u < VIPT; ++u) {
+        const int i = min(base + u * VBS + tid, n - 1);
+        const float4 h = hm[i], l = lo[i], w = wv[i];
+        xi[u] = (h.x - oh.x) + (l.x - ol.x);
+        yi[u] = (h.y - oh.y) + (l.y - ol.y);
+        zi[u] = (h.z - oh.z) + (l.z - ol.z);
+        mk[u] = h.w;
+        wkx[u] = w.x; wky[u] = w.y; wkz[u] = w.z;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s[u][q] = c[u][q] = 0.f;
+    }
+    f2x XI[VIPT], YI[VIPT], ZI[VIPT], MK[VIPT], WKX[VIPT], WKY[VIPT], WKZ[VIPT];
+#pragma unroll
+    for (int u = 0; u < VIPT; ++u) {
+        XI[u] = f2_bcast(xi[u]); YI[u] = f2_bcast(yi[u]); ZI[u] = f2_bcast(zi[u]);
+        MK[u] = f2_bcast(mk[u]);
+        WKX[u] = f2_bcast(wkx[u]); WKY[u] = f2_bcast(wky[u]); WKZ[u] = f2_bcast(wkz[u]);
+    }
+    const f2x E2 = f2_bcast(e2), C3 = f2_bcast(3.f);
+    for (int jt = j0; jt < j1; jt += VTILE) {
+        const int cnt = min(VTILE, j1 - jt);
+        const int cnt2 = (cnt + 1) & ~1;
+        __syncthreads();
+        for (int k = tid; k < cnt2; k += VBS) {
+            if (k < cnt) {
+                const float4 h = hm[jt + k], l = lo[jt + k], w = wv[jt + k];
+                sm.rx[k] = (h.x - oh.x) + (l.x - ol.x);
+                sm.ry[k] = (h.y - oh.y) + (l.y - ol.y);
+                sm.rz[k] = (h.z - oh.z) + (l.z - ol.z);
+                sm.rm[k] = h.w;
+                sm.wx[k] = w.x; sm.wy[k] = w.y; sm.wz[k] = w.z;
+            } else {
+                sm.rx[k] = sm.ry[k] = sm.rz[k] = 1e18f;  // far, massless, zero weight: adds nothing
+                sm.rm[k] = 0.f;
+                sm.wx[k] = sm.wy[k] = sm.wz[k] = 0.f;
+            }
+        }
+        __syncthreads();
+        f2x gx[VIPT], gy[VIPT], gz[VIPT], hh[VIPT];
+#pragma unroll
+        for (int u = 0; u < VIPT; ++u) gx[u] = gy[u] = gz[u] = hh[u] = 0ull;
+#pragma unroll 1
+        for (int k = 0; k < cnt2; k += 2) {
+            const f2x X = ld2(sm.rx + k), Y = ld2(sm.ry + k), Z = ld2(sm.rz + k), M = ld2(sm.rm + k);
+            const f2x WX = ld2(sm.wx + k), WY = ld2(sm.wy + k), WZ = ld2(sm.wz + k);
+#pragma unroll
+            for (int u = 0; u < VIPT; ++u) {
+                const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+                const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+                float ra, rb;
+                f2_unpack(r2, ra, rb);
+                float ia = rsqrt_mufu(ra), ib = rsqrt_mufu(rb);
+                if (EPS0) {
+                    ia = ra > 0.f ? ia : 0.f;
+                    ib = rb > 0.f ? ib : 0.f;
+                }
+                const f2x inv = f2_pack(ia, ib);
+                const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv2, inv), inv5 = f2_mul(inv3, inv2);
+                // u = m_k w_j - m_j w_k
+                const f2x ux = f2_sub(f2_mul(MK[u], WX), f2_mul(M, WKX[u]));
+                const f2x uy = f2_sub(f2_mul(MK[u], WY), f2_mul(M, WKY[u]));
+                const f2x uz = f2_sub(f2_mul(MK[u], WZ), f2_mul(M, WKZ[u]));
+                const f2x du = f2_fma(dx, ux, f2_fma(dy, uy, f2_mul(dz, uz)));
+                const f2x t = f2_mul(f2_mul(C3, du), inv5);
+                gx[u] = f2_sub(f2_fma(ux, inv3, gx[u]), f2_mul(dx, t));
+                gy[u] = f2_sub(f2_fma(uy, inv3, gy[u]), f2_mul(dy, t));
+                gz[u] = f2_sub(f2_fma(uz, inv3, gz[u]), f2_mul(dz, t));
+                const f2x wd = f2_fma(WX, dx, f2_fma(WY, dy, f2_mul(WZ, dz)));
+                hh[u] = f2_fma(wd, inv3, hh[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < VIPT; ++u) {
+            kahan_add(s[u][0], c[u][0], f2_sum(gx[u]));
+            kahan_add(s[u][1], c[u][1], f2_sum(gy[u]));
+            kahan_add(s[u][2], c[u][2], f2_sum(gz[u]));
+            kahan_add(s[u][3], c[u][3], f2_sum(hh[u]));
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < VIPT; ++u) {
+        const int i = base + u * VBS + tid;
+        if (i >= n) continue;
+        partial[static_cast<size_t>(blockIdx.y) * n + i] =
+            make_float4(s[u][0] - c[u][0], s[u][1] - c[u][1], s[u][2] - c[u][2], s[u][3] - c[u][3]);
+    }
+}
+
+// lx += G sum_slices g, lm -= G sum_slices h (slice order, FP64).
+__global__ void k_vjp_apply(const float4* __restrict__ partial, int n, int slices, double G, double* lx,
+                            double* ly, double* lz, double* lm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double g0 = 0, g1 = 0, g2 = 0, h = 0;
+    for (int k = 0; k < slices; ++k) {
+        const float4 p = partial[static_cast<size_t>(k) * n + i];
+        g0 += p.x; g1 += p.y; g2 += p.z; h += p.w;
+    }
+    lx[i] += G * g0;
+    ly[i] += G * g1;
+    lz[i] += G * g2;
+    lm[i] -= G * h;
+}
+
+// lv += dt lx; w = c lv (FP32 for the VJP), with the body's mass alongside.
+__global__ void k_adj_kick(const double* lx, const double* ly, const double* lz, double* lvx, double* lvy,
+                           double* lvz, double dt, double c, float4* w, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double vx = lvx[i] + dt * lx[i], vy = lvy[i] + dt * ly[i], vz = lvz[i] + dt * lz[i];
+    lvx[i] = vx; lvy[i] = vy; lvz[i] = vz;
+    w[i] = make_float4(static_cast<float>(c * vx), static_cast<float>(c * vy), static_cast<float>(c * vz), 0.f);
+}
+
+// Terminal adjoints from the final FP64 positions and the target (target indexed by id).
+__global__ void k_adj_init(const BodyArrays b, const double* tx, const double* ty, const double* tz, double* lx,
+                           double* ly, double* lz, double* lvx, double* lvy, double* lvz, double* lm, double* loss_terms,
+                           int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = b.id[i];
+    const double m = b.m[i];
+    const double dx = b.x[i] - tx[id], dy = b.y[i] - ty[id], dz = b.z[i] - tz[id];
+    lx[i] = 2 * m * dx; ly[i] = 2 * m * dy; lz[i] = 2 * m * dz;
+    lvx[i] = lvy[i] = lvz[i] = 0;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    lm[i] = d2;
+    loss_terms[i] = m * d2;
+}
+
+// Checkpoint copy of the state: FP64 positions, FP32 velocities.
+__global__ void k_save(const BodyArrays b, double* x, double* y, double* z, float* vx, float* vy, float* vz, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = b.x[i]; y[i] = b.y[i]; z[i] = b.z[i];
+    vx[i] = b.vx[i]; vy[i] = b.vy[i]; vz[i] = b.vz[i];
+}
+
+__global__ void k_restore(BodyArrays b, const double* x, const double* y, const double* z, const float* vx,
+                          const float* vy, const float* vz, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double px = x[i], py = y[i], pz = z[i];
+    b.x[i] = px; b.y[i] = py; b.z[i] = pz;
+    b.vx[i] = vx[i]; b.vy[i] = vy[i]; b.vz[i] = vz[i];
+    const float hx = __double2float_rn(px), hy = __double2float_rn(py), hz = __double2float_rn(pz);
+    b.hm[i] = make_float4(hx, hy, hz, b.m[i]);
+    b.lo[i] = make_float4(__double2float_rn(px - hx), __double2float_rn(py - hy), __double2float_rn(pz - hz), 0.f);
+}
+
+__global__ void k_copy_hilo(const BodyArrays b, float4* hm, float4* lo, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    hm[i] = b.hm[i];
+    lo[i] = b.lo[i];
+}
+
+}  // namespace
+
+// ---- host orchestration ------------------------------------------------------------------------
+struct AdjointState {
+    int n = 0, steps = 0, every = 0, nck = 0;
+    double dt = 0;
+    lg_force_params p{};
+    DevBuf ck_x, ck_y, ck_z, ck_vx, ck_vy, ck_vz;  // checkpoints, nck * n each
+    DevBuf seg_hm, seg_lo;                         // one segment's positions, (every + 1) * n float4
+    DevBuf lx, ly, lz, lvx, lvy, lvz, lm, loss_terms, w, partial;
+    DevBuf tx, ty, tz;
+    bool have_forward = false;
+};
+
+namespace {
+void destroy_adjoint(AdjointState* a) { delete a; }
+}  // namespace
+
+std::unique_ptr<AdjointState, void (*)(AdjointState*)> make_adjoint_state() {
+    return std::unique_ptr<AdjointState, void (*)(AdjointState*)>(new AdjointState, destroy_adjoint);
+}
+
+namespace {
+
+void save_ck(Engine& e, AdjointState& a, int slot) {
+    const size_t off = static_cast<size_t>(slot) * a.n;
+    k_save<<<grid_for(a.n, 256), 256, 0, e.stream>>>(e.bodies(e.cur), a.ck_x.as<double>() + off, a.ck_y.as<double>() + off,
+                                                   a.ck_z.as<double>() + off, a.ck_vx.as<float>() + off,
+                                                   a.ck_vy.as<float>() + off, a.ck_vz.as<float>() + off, a.n);
+    LG_LAUNCHED();
+    ++e.launches;
+}
+
+void direct_forces(Engine& e, const lg_force_params& p) {
+    const float G = static_cast<float>(p.G), e2 = static_cast<float>(p.eps * p.eps);
+    const bool eps0 = !(e2 >= 1.17549435e-38f);
+    DirectShape sh = e.direct_shape_override.ipt ? e.direct_shape_override : default_direct_shape(e.n, e.sms);
+    if (sh.slices > 1) e.partial.reserve(static_cast<size_t>(sh.slices) * e.n * 16 + 16 * 1024);
+    launch_direct(e.bodies(e.cur), e.n, G, e2, false, eps0, sh, e.acc.as<float4>(), e.partial.as<float4>(), e.err_word(),
+                  e.stream);
+    e.launches += sh.slices > 1 ? 2 : 1;
+}
+
+void kdk_step(Engine& e, const lg_force_params& p, double dt) {
+    launch_kick(e.bodies(e.cur), e.acc.as<float4>(), static_cast<float>(0.5 * dt), e.n, e.stream);
+    launch_drift(e.bodies(e.cur), dt, e.n, e.stream);
+    direct_forces(e, p);
+    launch_kick(e.bodies(e.cur), e.acc.as<float4>(), static_cast<float>(0.5 * dt), e.n, e.stream);
+    e.launches += 3;
+}
+
+}  // namespace
+
+void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every) {
+    if (p.method != LG_DIRECT) fail(kRuntime, "adjoint: only the direct method is supported");
+    if (steps < 1 || every < 1) fail(kArg, "adjoint: steps and checkpoint interval must be positive");
+    LG_CK(cudaSetDevice(e.dev));
+    const int n = e.n;
+    if (n < 1) fail(kArg, "adjoint: no bodies");
+    a.n = n;
+    a.steps = steps;
+    a.every = every;
+    a.dt = dt;
+    a.p = p;
+    a.nck = (steps + every - 1) / every + 1;
+    const size_t cn = static_cast<size_t>(a.nck) * n;
+    a.ck_x.reserve(cn * 8); a.ck_y.reserve(cn * 8); a.ck_z.reserve(cn * 8);
+    a.ck_vx.reserve(cn * 4); a.ck_vy.reserve(cn * 4); a.ck_vz.reserve(cn * 4);
+    direct_forces(e, p);
+    save_ck(e, a, 0);
+    for (int s = 0; s < steps; ++s) {
+        kdk_step(e, p, dt);
+        if ((s + 1) % every == 0 && s + 1 < steps) save_ck(e, a, (s + 1) / every);
+    }
+    e.acc_ok = true;
+    e.has_pe = false;
+    e.tree_ok = false;
+    e.costs_ok = false;
+    a.have_forward = true;
+    LG_CK(cudaStreamSynchronize(e.stream));
+    e.check_device_errors("adjoint forward");
+}
+
+double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const double* ty, const double* tz, double* gx,
+                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm) {
+    if (!a.have_forward || a.n != e.n) fail(kLogic, "adjoint backward: run the adjoint forward pass first");
+    LG_CK(cudaSetDevice(e.dev));
+    const int n = a.n;
+    cudaStream_t s = e.stream;
+    const size_t nb8 = static_cast<size_t>(n) * 8;
+    for (DevBuf* d : {&a.lx, &a.ly, &a.lz, &a.lvx, &a.lvy, &a.lvz, &a.lm, &a.loss_terms, &a.tx, &a.ty, &a.tz})
+        d->reserve(nb8);
+    a.w.reserve(static_cast<size_t>(n) * 16);
+    a.seg_hm.reserve(static_cast<size_t>(a.every + 1) * n * 16);
+    a.seg_lo.reserve(static_cast<size_t>(a.every + 1) * n * 16);
+    LG_CK(cudaMemcpyAsync(a.tx.as<double>(), tx, nb8, cudaMemcpyHostToDevice, s));
+    LG_CK(cudaMemcpyAsync(a.ty.as<double>(), ty, nb8, cudaMemcpyHostToDevice, s));
+    LG_CK(cudaMemcpyAsync(a.tz.as<double>(), tz, nb8, cudaMemcpyHostToDevice, s));
+    const int gb = grid_for(n, 256);
+    // The forward pass left the final state resident: terminal adjoints from it.
+    k_adj_init<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
+                                  a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                  a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(), a.loss_terms.as<double>(), n);
+    LG_LAUNCHED();
+    std::vector<double> terms(static_cast<size_t>(n));
+    LG_CK(cudaMemcpyAsync(terms.data(), a.loss_terms.as<double>(), nb8, cudaMemcpyDeviceToHost, s));
+    // VJP launch shape: whole waves over split-j slices.
+    const int iblocks = (n + VBS * VIPT - 1) / (VBS * VIPT);
+    int slices = std::max(1, std::min(n / 128 + 1, (2 * e.sms + iblocks - 1) / iblocks));
+    int jslice = (n + slices - 1) / slices;
+    slices = (n + jslice - 1) / jslice;
+    a.partial.reserve(static_cast<size_t>(slices) * n * 16);
+    const float e2 = static_cast<float>(a.p.eps * a.p.eps);
+    const bool eps0 = !(e2 >= 1.17549435e-38f);
+    const double h = 0.5 * a.dt;
+    for (int seg = (a.steps - 1) / a.every; seg >= 0; --seg) {
+        const int s0 = seg * a.every, s1 = std::min(a.steps, s0 + a.every);
+        // Restore the checkpoint at s0 and recompute the segment's positions.
+        const size_t off = static_cast<size_t>(seg) * n;
+        k_restore<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.ck_x.as<double>() + off, a.ck_y.as<double>() + off,
+                                     a.ck_z.as<double>() + off, a.ck_vx.as<float>() + off, a.ck_vy.as<float>() + off,
+                                     a.ck_vz.as<float>() + off, n);
+        LG_LAUNCHED();
+        direct_forces(e, a.p);
+        k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>(), a.seg_lo.as<float4>(), n);
+        LG_LAUNCHED();
+        for (int st = s0; st < s1 - 1; ++st) {
+            kdk_step(e, a.p, a.dt);
+            const size_t so = static_cast<size_t>(st - s0 + 1) * n;
+            k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, n);
+            LG_LAUNCHED();
+        }
+        e.launches += 2 + (s1 - 1 - s0);
+        // Reverse through the segment.
+        for (int st = s1 - 1; st >= s0; --st) {
+            const double c = st > 0 ? a.dt : h;
+            k_adj_kick<<<gb, 256, 0, s>>>(a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                          a.lvy.as<double>(), a.lvz.as<double>(), a.dt, c, a.w.as<float4>(), n);
+            LG_LAUNCHED();
+            const size_t so = static_cast<size_t>(st - s0) * n;
+            dim3 grid(iblocks, slices);
+            if (eps0)
+                k_vjp<true><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, a.w.as<float4>(), n,
+                                                 jslice, e2, a.partial.as<float4>());
+            else
+                k_vjp<false><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, a.w.as<float4>(),
+                                                  n, jslice, e2, a.partial.as<float4>());
+            LG_LAUNCHED();
+            k_vjp_apply<<<gb, 256, 0, s>>>(a.partial.as<float4>(), n, slices, a.p.G, a.lx.as<double>(), a.ly.as<double>(),
+                                           a.lz.as<double>(), a.lm.as<double>());
+            LG_LAUNCHED();
+            e.launches += 3;
+        }
+    }
+    // Gradients in id order.
+    std::vector<uint32_t> ids(static_cast<size_t>(n));
+    LG_CK(cudaMemcpyAsync(ids.data(), e.bodies(e.cur).id, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost, s));
+    std::vector<double> buf(static_cast<size_t>(n) * 7);
+    DevBuf* outs[7] = {&a.lx, &a.ly, &a.lz, &a.lvx, &a.lvy, &a.lvz, &a.lm};
+    for (int k = 0; k < 7; ++k)
+        LG_CK(cudaMemcpyAsync(buf.data() + static_cast<size_t>(k) * n, outs[k]->as<double>(), nb8, cudaMemcpyDeviceToHost, s));
+    LG_CK(cudaStreamSynchronize(s));
+    e.check_device_errors("adjoint backward");
+    double* dst[7] = {gx, gy, gz, gvx, gvy, gvz, gm};
+    for (int k = 0; k < 7; ++k)
+        if (dst[k])
+            for (int i = 0; i < n; ++i) dst[k][ids[i]] = buf[static_cast<size_t>(k) * n + i];
+    double L = 0;
+    for (double t : terms) L += t;
+    // The backward pass restored and replayed segment 0 only in part: the resident state is the
+    // first segment's, so the forward result is no longer resident.
+    a.have_forward = false;
+    e.acc_ok = false;
+    return L;
+}
+
+}  // namespace lg

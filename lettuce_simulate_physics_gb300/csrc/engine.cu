@@ -67,12 +67,14 @@ Engine::Engine(int device) : dev(device) {
     pinned_small = nullptr;
     LG_CK(cudaMallocHost(&pinned_small, 4096));
     tree = make_tree_state();
+    adjoint = make_adjoint_state();
 }
 
 Engine::~Engine() {
     cudaSetDevice(dev);
     if (stream) cudaStreamSynchronize(stream);
     tree.reset();
+    adjoint.reset();
     for (auto& ev : events) if (ev) cudaEventDestroy(ev);
     for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
     if (pinned_small) cudaFreeHost(pinned_small);
@@ -662,6 +664,26 @@ lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops) {
         Engine& E = eng(e);
         LG_CK(cudaSetDevice(E.dev));
         *tflops = lg::probe_fp32_peak(E.stream, E.sms, E.err_word() + 12);
+    });
+}
+
+lg_status lg_adjoint_forward(lg_engine* e, const lg_force_params* p, double dt, int steps, int checkpoint_every) {
+    return guard([&] {
+        need(p, "params");
+        Engine& E = eng(e);
+        lg::adjoint_forward(E, *E.adjoint, *p, dt, steps, checkpoint_every);
+    });
+}
+
+lg_status lg_adjoint_backward(lg_engine* e, const double* tx, const double* ty, const double* tz, double* loss,
+                              double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm) {
+    return guard([&] {
+        need(tx, "target_x");
+        need(ty, "target_y");
+        need(tz, "target_z");
+        Engine& E = eng(e);
+        const double L = lg::adjoint_backward(E, *E.adjoint, tx, ty, tz, gx, gy, gz, gvx, gvy, gvz, gm);
+        if (loss) *loss = L;
     });
 }
 

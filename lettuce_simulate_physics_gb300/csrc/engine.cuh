@@ -11,7 +11,8 @@
 
 namespace lg {
 
-struct TreeState;  // tree.cu
+struct TreeState;     // tree.cu
+struct AdjointState;  // adjoint.cu
 
 // Read-only view of the built tree for the walk.
 struct TreeView {
@@ -95,6 +96,7 @@ struct Engine {
     uint64_t launches = 0;
     uint64_t last_body_pairs = 0, last_cell_terms = 0;
     std::unique_ptr<TreeState, void (*)(TreeState*)> tree{nullptr, nullptr};
+    std::unique_ptr<AdjointState, void (*)(AdjointState*)> adjoint{nullptr, nullptr};
 };
 
 extern thread_local std::string g_last_error;
@@ -113,6 +115,11 @@ lg_memory_estimate memory_need(uint64_t n, int method);
 const void* probe_kernel();
 // walk.cu
 void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0);
+// adjoint.cu
+std::unique_ptr<AdjointState, void (*)(AdjointState*)> make_adjoint_state();
+void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every);
+double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const double* ty, const double* tz, double* gx,
+                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm);
 // integrate.cu
 double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink);
 
