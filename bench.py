@@ -154,6 +154,55 @@ def force_error_sample(be, b, w, count=256, seed=7):
     return float(np.median(errs)), float(np.percentile(errs, 99))
 
 
+def adjoint_leg(L, local, steps=1000, every=32, n=65536):
+    """Adjoint of the direct-sum leapfrog at the configuration-2 shape: Plummer N=65536 (seed 2),
+    eps 0.01, dt 1e-3, 1000 KDK steps, checkpoints every 32; target x* from a forward run whose
+    initial positions carry Gaussian perturbations (sigma 1e-3). Returns forward and adjoint device
+    milliseconds per step and their ratio."""
+    from lettuce_simulate_physics_gb300 import scenarios as S
+    be = L.CudaBackend(local)
+    p = L.ForceParams(G=1.0, eps=0.01, method=L.ForceMethod.direct)
+    dt = 1e-3
+    b = S.plummer(n, 2, cut=10)
+    rng = np.random.Generator(np.random.PCG64(2))
+    bp = b.copy()
+    bp.x += rng.normal(0, 1e-3, n).astype(np.float32)
+    bp.y += rng.normal(0, 1e-3, n).astype(np.float32)
+    bp.z += rng.normal(0, 1e-3, n).astype(np.float32)
+    # Target: forward run of the perturbed initial conditions (plain steps).
+    be.upload(bp)
+    be.compute_forces(p, False)
+    be.synchronize()
+    be.event_record(2)
+    for _ in range(steps):
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        be.kick(0.5 * dt)
+    be.event_record(3)
+    fwd_ms = be.event_elapsed(2, 3) / steps
+    pos = be.pos64()
+    ids = be.download().id
+    xstar = np.zeros((n, 3))
+    xstar[ids] = pos.T
+    be.upload(b)
+    be.synchronize()
+    be.event_record(4)
+    be.adjoint_forward(p, dt, steps, every)
+    be.event_record(5)
+    ck_fwd_ms = be.event_elapsed(4, 5) / steps
+    be.event_record(6)
+    loss, gx, gv, gm = be.adjoint_backward(xstar)
+    be.event_record(7)
+    adj_ms = be.event_elapsed(6, 7) / steps
+    be.close()
+    return {"n": n, "steps": steps, "checkpoint_every": every, "loss": loss,
+            "forward_ms_per_step": round(fwd_ms, 4), "checkpointed_forward_ms_per_step": round(ck_fwd_ms, 4),
+            "adjoint_ms_per_step": round(adj_ms, 4), "adjoint_over_forward": round(adj_ms / fwd_ms, 3),
+            "grad_norms": {"x": float(np.linalg.norm(gx)), "v": float(np.linalg.norm(gv)),
+                           "m": float(np.linalg.norm(gm))}}
+
+
 def read_profile_traffic(workload):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -294,6 +343,10 @@ def run_gb300(args, w, world, rank, local, dist):
         cpu = {"value": round(cms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
                "sample": f"{args.ref_steps} KDK step(s) of the full workload (N={n}) after one warm-up force call"}
 
+    adj = None
+    if rank == 0 and not args.no_adjoint:
+        adj = adjoint_leg(L, local, steps=args.adjoint_steps)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
@@ -313,6 +366,7 @@ def run_gb300(args, w, world, rank, local, dist):
                          "peak_source": "measured FFMA throughput on this GPU (lg_probe_fp32_peak)",
                          "flops_per_unit": {"body_pair": 20, "cell_term": 65}},
             "cpu_baseline": cpu,
+            "adjoint": adj,
             "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": int(launches),
@@ -333,6 +387,8 @@ def main():
     ap.add_argument("--workload", default="disk1m", choices=sorted(WORKLOADS))
     ap.add_argument("--ref-steps", type=int, default=2, help="KDK steps timed on the CPU")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--adjoint-steps", type=int, default=1000, help="KDK steps of the adjoint leg")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     world, rank, local, dist = dist_setup()
