@@ -116,6 +116,7 @@ void Engine::upload(size_t count, const float* x, const float* y, const float* z
     costs_ok = false;
     kick_rec = drift_rec = false;
     times = lg_phase_times{};
+    tree_reset_guess(*this);
     if (n == 0) return;
     const size_t fb = count * 4;
     BodyArrays b = bodies(0);
@@ -182,6 +183,17 @@ void Engine::check_device_errors(const char* where) {
     }
 }
 
+void Engine::ensure_tree_valid() {
+    if (!tree_ok) return;
+    LG_CK(cudaMemcpyAsync(pinned_small + 64, tree_counts_device(*this), 32, cudaMemcpyDeviceToHost, stream));
+    LG_CK(cudaStreamSynchronize(stream));
+    if (tree_verify(*this, pinned_small + 64)) return;
+    lg_force_params p{};
+    p.method = LG_TREE;
+    p.theta = tree_theta(*this);
+    build_tree(p);  // exact sizes now; invalidates the accelerations as any build does
+}
+
 void Engine::build_tree(const lg_force_params& p) {
     LG_CK(cudaSetDevice(dev));
     tree_ok = false;
@@ -236,7 +248,16 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
     }
     LG_CK(cudaEventRecord(events[EV_WALK1], stream));
     LG_CK(cudaMemcpyAsync(pinned_small, small.as<char>(), 128, cudaMemcpyDeviceToHost, stream));
+    if (tree_m) LG_CK(cudaMemcpyAsync(pinned_small + 64, tree_counts_device(*this), 32, cudaMemcpyDeviceToHost, stream));
     LG_CK(cudaStreamSynchronize(stream));
+    if (tree_m && !tree_verify(*this, pinned_small + 64)) {
+        // A sync-free build guessed its sizes wrong (or missed a key restart): rebuild exactly and
+        // walk again. The bodies are already sorted, so the stable re-sort keeps their order.
+        LG_CK(cudaMemsetAsync(err_word(), 0, 4, stream));
+        build_tree(p);
+        compute_forces_with(p, potential, nremote);
+        return;
+    }
     check_device_errors(tree_m ? "cuda tree walk" : "cuda direct");
     times.sort_ms = tree_m && pend_tree_times ? elapsed(EV_BUILD0, EV_SORTED) : 0.0;
     times.build_ms = tree_m && pend_tree_times ? elapsed(EV_SORTED, EV_BUILT) : 0.0;

@@ -61,6 +61,7 @@ struct Engine {
     double* dscratch() const;
     float elapsed(int a, int b) const;
     void check_device_errors(const char* where);
+    void ensure_tree_valid();  // rebuilds exactly if a sync-free build guessed wrong
 
     // Device, stream, events.
     int dev = 0;
@@ -107,6 +108,10 @@ void tree_sort(Engine& e);                    // keys, radix sort, permute (+ ke
 void tree_build(Engine& e, double theta);     // octree, groups, moments
 size_t tree_held_bytes(const Engine& e);
 TreeView tree_view(Engine& e);
+bool tree_verify(Engine& e, const unsigned* counts_host);
+const unsigned* tree_counts_device(Engine& e);
+void tree_reset_guess(Engine& e);
+double tree_theta(const Engine& e);
 void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth);
 void tree_keys(Engine& e, uint64_t* keys, size_t n);
 void tree_nodes(Engine& e, uint32_t* lohi_first_nchild, float* moments11, float* geo4, size_t nodes);

@@ -83,10 +83,15 @@ struct TreeState {
     DevBuf ups, dep_nodes, leaf_order;
     // scan state
     DevBuf scan_state, scan_ctr;
-    size_t K = 0, T = 0, ngroups = 0, nruns = 0;
+    size_t K = 0, T = 0, ngroups = 0, nruns = 0;  // sizes the last build was launched with
     int max_depth = 0;
     bool restarted = false;
     int group_max = 128;
+    // Sync-free builds: sizes from the previous build with headroom; verified after the walk.
+    bool have_guess = false;
+    bool restart_mode = false;  // key restarts were needed last time: check for them on the host
+    bool speculative = false;   // the current build used guessed sizes / assumed no restart
+    double theta = 0.6;
 };
 
 namespace {
@@ -637,8 +642,13 @@ struct NodeCtx {
     const uint32_t* leaf_pre;    // K+1
     const uint32_t* lid;         // per body
     const uint16_t* bdepth;
-    int n, K;
+    int n;
+    const unsigned* Kdev;  // leaf count (device)
+    unsigned Kcap;         // capacity the leaf arrays were sized for
 };
+
+__device__ __forceinline__ int leaf_count(const NodeCtx& c) { return static_cast<int>(min(*c.Kdev, c.Kcap)); }
+__device__ __forceinline__ uint32_t eff(const unsigned* dev, uint32_t cap) { return min(*dev, cap); }
 
 // Pre-order index of the node at depth d whose first body is b (b must start that node).
 __device__ __forceinline__ uint32_t node_at(const NodeCtx& c, uint32_t b, int d) {
@@ -658,11 +668,11 @@ __device__ __forceinline__ uint32_t range_end(const NodeCtx& c, uint32_t lo, int
 }
 
 // Per pre-order node: (lo, hi) and meta = depth | leaf << 8 | group << 9.
-__global__ void k_nodes_pre(NodeCtx c, uint32_t T, uint2* pn_lohi, uint16_t* pn_meta) {
+__global__ void k_nodes_pre(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, uint2* pn_lohi, uint16_t* pn_meta) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= T) return;
+    if (v >= eff(Tdev, Tcap)) return;
     // Leaf owning v: last l with leaf_pre[l] <= v.
-    int a = 0, b = c.K;
+    int a = 0, b = leaf_count(c);
     while (b - a > 1) {
         int mid = (a + b) >> 1;
         if (c.leaf_pre[mid] <= v) a = mid;
@@ -696,19 +706,24 @@ __device__ __forceinline__ int for_children(const NodeCtx& c, const uint2* pn_lo
     return k;
 }
 
-__global__ void k_nchild(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta, uint32_t* pn_nchild) {
+__global__ void k_nchild(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, const uint2* pn_lohi, const uint16_t* pn_meta,
+                         uint32_t* pn_nchild) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= T) return;
+    if (v >= Tcap) return;
+    if (v >= eff(Tdev, Tcap)) {
+        pn_nchild[v] = 0;  // scanned over the capacity
+        return;
+    }
     const uint16_t meta = pn_meta[v];
     int k = 0;
     if (!(meta & 256)) k = for_children(c, pn_lohi, v, meta & 255, [](int, uint32_t) {});
     pn_nchild[v] = static_cast<uint32_t>(k);
 }
 
-__global__ void k_cpu_index(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta,
-                            const uint32_t* pn_cb, uint32_t* pn_cpu) {
+__global__ void k_cpu_index(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, const uint2* pn_lohi,
+                            const uint16_t* pn_meta, const uint32_t* pn_cb, uint32_t* pn_cpu) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= T) return;
+    if (v >= eff(Tdev, Tcap)) return;
     if (v == 0) pn_cpu[0] = 0;
     const uint16_t meta = pn_meta[v];
     if (meta & 256) return;
@@ -743,12 +758,13 @@ __device__ void node_geo(const NodeCtx& c, const double* frame, const int* runid
     }
 }
 
-__global__ void k_nodes_out(NodeCtx c, uint32_t T, const uint2* pn_lohi, const uint16_t* pn_meta,
+__global__ void k_nodes_out(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, const uint2* pn_lohi, const uint16_t* pn_meta,
                             const uint32_t* pn_nchild, const uint32_t* pn_cb, const uint32_t* pn_cpu,
                             const double* frame, const int* runid, const double* cube, uint4* nd_range,
                             float4* nd_geo, uint32_t* nd_parent, uint32_t* leaf_node, const uint32_t* gidx,
                             uint32_t* grp_node, int* max_depth, unsigned* err) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t T = eff(Tdev, Tcap);
     if (v >= T) return;
     const uint16_t meta = pn_meta[v];
     const int d = meta & 255;
@@ -771,7 +787,7 @@ __global__ void k_nodes_out(NodeCtx c, uint32_t T, const uint2* pn_lohi, const u
         for (uint32_t k = 0; k < nch; ++k) nd_parent[first + k] = me;
     if (leaf) {
         const uint32_t l = c.lid[r.x];
-        if (l < static_cast<uint32_t>(c.K)) leaf_node[l] = me;
+        if (l < static_cast<uint32_t>(leaf_count(c))) leaf_node[l] = me;
         else atomicOr(err, kErrNodeOverflow);
     }
     if (meta & 512) {
@@ -783,10 +799,11 @@ __global__ void k_nodes_out(NodeCtx c, uint32_t T, const uint2* pn_lohi, const u
 }
 
 // Group boxes from the bodies' float positions (src/cpu_backend.cpp:604-616).
-__global__ void k_groups(const uint32_t* grp_node, const uint2* pn_lohi, uint32_t T, const BodyArrays b,
-                         const unsigned* ngroups, uint2* grp_range, float4* grp_box) {
+__global__ void k_groups(const uint32_t* grp_node, const uint2* pn_lohi, uint32_t Tcap, const unsigned* Tdev,
+                         const BodyArrays b, const unsigned* ngroups, uint2* grp_range, float4* grp_box) {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= *ngroups) return;
+    const uint32_t T = eff(Tdev, Tcap);
+    if (g >= *ngroups || g >= Tcap) return;
     const uint32_t v = grp_node[g];
     if (v >= T) return;
     const uint2 r = pn_lohi[v];
@@ -849,8 +866,10 @@ struct UpsweepIndex {
 __device__ __forceinline__ int lsz_bucket(uint32_t cnt) { return cnt > 16 ? 17 : static_cast<int>(cnt); }
 
 // Pass 1: bucket counts (block-aggregated). Pass 2 (phase 1): scatter into bucket order.
-__global__ void k_upsweep_bucket(const uint2* pn_lohi, const uint16_t* pn_meta, const uint32_t* pn_cpu, uint32_t T,
-                                 UpsweepIndex* ix, int phase, uint32_t* dep_nodes, uint32_t* leaf_order) {
+__global__ void k_upsweep_bucket(const uint2* pn_lohi, const uint16_t* pn_meta, const uint32_t* pn_cpu, uint32_t Tcap,
+                                 const unsigned* Tdev, UpsweepIndex* ix, int phase, uint32_t* dep_nodes,
+                                 uint32_t* leaf_order) {
+    const uint32_t T = eff(Tdev, Tcap);
     __shared__ unsigned sc[NDEP + NLSZ], sbase[NDEP + NLSZ];
     for (int k = threadIdx.x; k < NDEP + NLSZ; k += blockDim.x) sc[k] = 0;
     __syncthreads();
@@ -899,11 +918,13 @@ __global__ void k_upsweep_offsets(UpsweepIndex* ix) {
 
 // Leaf moments about each leaf's centre of mass in FP64 (src/cpu_backend.cpp:619-640), one
 // thread per leaf, leaves taken in body-count order so a warp's loops have equal trip counts.
-__global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t K, uint32_t T,
-                               const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo, const BodyArrays b,
-                               Moments mo, float inv_theta, unsigned* err) {
+__global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t Kcap, const unsigned* Kdev,
+                               uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
+                               const float4* __restrict__ nd_geo, const BodyArrays b, Moments mo, float inv_theta,
+                               unsigned* err) {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= K) return;
+    const uint32_t T = eff(Tdev, Tcap);
+    if (l >= eff(Kdev, Kcap)) return;
     const uint32_t node = leaf_order[l];
     if (node >= T) {
         atomicOr(err, kErrNodeOverflow);
@@ -938,9 +959,10 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
 
 // Internal nodes of one depth: combine the children (already final) in index order, FP64, the
 // parallel-axis theorem for the traceless quadrupole (src/cpu_backend.cpp:642-663).
-__global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth, uint32_t T,
-                                const uint4* __restrict__ nd_range, const float4* __restrict__ nd_geo, Moments mo,
-                                float inv_theta, unsigned* err) {
+__global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth,
+                                uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
+                                const float4* __restrict__ nd_geo, Moments mo, float inv_theta, unsigned* err) {
+    const uint32_t T = eff(Tdev, Tcap);
     const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
     for (unsigned k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
         const uint32_t p = dep_nodes[k];
@@ -997,9 +1019,9 @@ __global__ void k_lid(uint32_t* lid, const uint32_t* flag, int n) {
 
 __global__ void k_leaf_tail(uint32_t* leaf_first, const unsigned* K, int n) { leaf_first[*K] = static_cast<uint32_t>(n); }
 
-__global__ void k_gflag(const uint16_t* pn_meta, uint32_t T, uint32_t* gflag) {
+__global__ void k_gflag(const uint16_t* pn_meta, uint32_t Tcap, const unsigned* Tdev, uint32_t* gflag) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < T) gflag[v] = (pn_meta[v] >> 9) & 1u;
+    if (v < Tcap) gflag[v] = v < eff(Tdev, Tcap) ? (pn_meta[v] >> 9) & 1u : 0u;
 }
 
 __global__ void k_probe() {}
@@ -1095,9 +1117,14 @@ void tree_sort(Engine& e) {
     k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), n, t.runs.as<uint2>(), counts, run_cap);
     LG_LAUNCHED();
     ++e.launches;
+    // Key restarts are rare: unless the last build needed them, assume none and let the check after
+    // the walk (tree_verify) catch a miss; otherwise read the run count now.
+    t.speculative = t.have_guess && !t.restart_mode;
+    if (t.speculative) return;
     LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 4, cudaMemcpyDeviceToHost, s));
     LG_CK(cudaStreamSynchronize(s));
     const unsigned R = e.pinned_small[0];
+    t.restart_mode = R > 0;
     if (R == 0) return;
     t.nruns = R;
     t.restarted = true;
@@ -1140,11 +1167,14 @@ void tree_build(Engine& e, double theta) {
     const int n = e.n;
     cudaStream_t s = e.stream;
     t.group_max = e.group_max;
+    t.theta = theta;
     const uint64_t* k0 = t.skey.as<uint64_t>();
     const uint64_t* k1 = t.restarted ? t.skey1.as<uint64_t>() : nullptr;
     const int* runid = t.restarted ? t.runid.as<int>() : nullptr;
     const double* cube = t.restarted ? t.runcube.as<double>() : nullptr;
     unsigned* counts = t.counts.as<unsigned>();
+    const unsigned* Kdev = counts + 1;
+    const unsigned* Tdev = counts + 2;
     const size_t n1 = static_cast<size_t>(n) + 1;
     t.bdepth.reserve(n1 * 2);
     t.flag.reserve(n1 * 4);
@@ -1174,14 +1204,32 @@ void tree_build(Engine& e, double theta) {
     LG_LAUNCHED();
     e.launches += 3;
     scan_u32(e, t, t.leaf_cnt.as<uint32_t>(), t.leaf_pre.as<uint32_t>(), n + 1, counts + 2);
-    LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 32, cudaMemcpyDeviceToHost, s));
-    LG_CK(cudaStreamSynchronize(s));
-    t.K = e.pinned_small[1];
-    t.T = e.pinned_small[2];
-    t.max_depth = static_cast<int>(e.pinned_small[4]);
-    const size_t K = t.K, T = t.T;
-    if (K < 1 || K > static_cast<size_t>(n) || T < K)
-        fail(kRuntime, "cuda tree build: bad leaf/node count " + std::to_string(K) + "/" + std::to_string(T));
+    // Sizes: exact (one host read) for the first build and after a miss; otherwise the previous
+    // build's with headroom, checked by tree_verify once the force call synchronises.
+    size_t K, T;
+    int depth;
+    const bool spec = t.have_guess && (t.speculative || t.restarted);
+    if (spec) {
+        K = t.K;
+        T = t.T;
+        depth = t.max_depth;
+        t.speculative = true;
+    } else {
+        LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 32, cudaMemcpyDeviceToHost, s));
+        LG_CK(cudaStreamSynchronize(s));
+        const size_t Kx = e.pinned_small[1], Tx = e.pinned_small[2];
+        const int dx = static_cast<int>(e.pinned_small[4]);
+        if (Kx < 1 || Kx > static_cast<size_t>(n) || Tx < Kx)
+            fail(kRuntime, "cuda tree build: bad leaf/node count " + std::to_string(Kx) + "/" + std::to_string(Tx));
+        K = std::min(static_cast<size_t>(n), Kx + Kx / 4 + 1024);
+        T = Tx + Tx / 4 + 1024;
+        depth = std::min(dx + 2, MAX_DEPTH + 1);
+        t.K = K;
+        t.T = T;
+        t.max_depth = depth;
+        t.have_guess = true;
+        t.speculative = false;
+    }
     t.pn_lohi.reserve(T * 8);
     t.pn_meta.reserve(T * 2);
     t.pn_nchild.reserve(T * 4);
@@ -1194,9 +1242,9 @@ void tree_build(Engine& e, double theta) {
     t.grp_box.reserve(T * 32);
     for (DevBuf* d : {&t.nd_range, &t.nd_com, &t.nd_comlo, &t.nd_q0, &t.nd_q1, &t.nd_geo}) d->reserve(T * 16);
     t.nd_parent.reserve(T * 4);
-    t.nd_arrive.reserve(T * 4);
+    const uint32_t Tc = static_cast<uint32_t>(T), Kc = static_cast<uint32_t>(K);
     NodeCtx c{k0, k1, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
-              t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, static_cast<int>(K)};
+              t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, Kdev, Kc};
     const int tb = grid_for(static_cast<long long>(T), BS);
     // Index arrays start out of range (0xff..): a slot the construction fails to fill is caught by
     // the range checks below instead of being followed.
@@ -1206,60 +1254,81 @@ void tree_build(Engine& e, double theta) {
     LG_CK(cudaMemsetAsync(t.nd_parent.as<char>(), 0xff, T * 4, s));
     LG_CK(cudaMemsetAsync(t.nd_range.as<char>(), 0, T * 16, s));
     LG_CK(cudaMemsetAsync(t.grp_range.as<char>(), 0, T * 8, s));
-    k_nodes_pre<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>());
+    k_nodes_pre<<<tb, BS, 0, s>>>(c, Tc, Tdev, t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>());
     LG_LAUNCHED();
-    k_nchild<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
-                               t.pn_nchild.as<uint32_t>());
+    k_nchild<<<tb, BS, 0, s>>>(c, Tc, Tdev, t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_nchild.as<uint32_t>());
     LG_LAUNCHED();
     e.launches += 2;
     scan_u32(e, t, t.pn_nchild.as<uint32_t>(), t.pn_cb.as<uint32_t>(), static_cast<int>(T), nullptr);
-    k_gflag<<<tb, BS, 0, s>>>(t.pn_meta.as<uint16_t>(), static_cast<uint32_t>(T), t.gflag.as<uint32_t>());
+    k_gflag<<<tb, BS, 0, s>>>(t.pn_meta.as<uint16_t>(), Tc, Tdev, t.gflag.as<uint32_t>());
     LG_LAUNCHED();
     ++e.launches;
     scan_u32(e, t, t.gflag.as<uint32_t>(), t.gidx.as<uint32_t>(), static_cast<int>(T), counts + 3);
-    k_cpu_index<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
-                                  t.pn_cb.as<uint32_t>(), t.pn_cpu.as<uint32_t>());
+    k_cpu_index<<<tb, BS, 0, s>>>(c, Tc, Tdev, t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cb.as<uint32_t>(),
+                                  t.pn_cpu.as<uint32_t>());
     LG_LAUNCHED();
-    k_nodes_out<<<tb, BS, 0, s>>>(c, static_cast<uint32_t>(T), t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
+    k_nodes_out<<<tb, BS, 0, s>>>(c, Tc, Tdev, t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
                                   t.pn_nchild.as<uint32_t>(), t.pn_cb.as<uint32_t>(), t.pn_cpu.as<uint32_t>(),
                                   t.frame.as<double>(), runid, cube, t.nd_range.as<uint4>(), t.nd_geo.as<float4>(),
                                   t.nd_parent.as<uint32_t>(), t.leaf_node.as<uint32_t>(), t.gidx.as<uint32_t>(),
                                   t.grp_node.as<uint32_t>(), reinterpret_cast<int*>(counts + 4), e.err_word());
     LG_LAUNCHED();
-    k_groups<<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_lohi.as<uint2>(), static_cast<uint32_t>(T),
-                               e.bodies(e.cur), counts + 3,
+    k_groups<<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_lohi.as<uint2>(), Tc, Tdev, e.bodies(e.cur), counts + 3,
                                t.grp_range.as<uint2>(), t.grp_box.as<float4>());
     LG_LAUNCHED();
+    e.launches += 3;
     // Upsweep: leaves (by size), then internal nodes level by level from the deepest.
     t.ups.reserve(sizeof(UpsweepIndex));
     t.dep_nodes.reserve(T * 4);
     t.leaf_order.reserve(K * 4);
     UpsweepIndex* ix = t.ups.as<UpsweepIndex>();
     LG_CK(cudaMemsetAsync(ix, 0, sizeof(UpsweepIndex), s));
-    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(),
-                                       static_cast<uint32_t>(T), ix, 0, nullptr, nullptr);
+    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(), Tc, Tdev,
+                                       ix, 0, nullptr, nullptr);
     LG_LAUNCHED();
     k_upsweep_offsets<<<1, 32, 0, s>>>(ix);
     LG_LAUNCHED();
-    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(),
-                                       static_cast<uint32_t>(T), ix, 1, t.dep_nodes.as<uint32_t>(),
-                                       t.leaf_order.as<uint32_t>());
+    k_upsweep_bucket<<<tb, BS, 0, s>>>(t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(), t.pn_cpu.as<uint32_t>(), Tc, Tdev,
+                                       ix, 1, t.dep_nodes.as<uint32_t>(), t.leaf_order.as<uint32_t>());
     LG_LAUNCHED();
     const float inv_theta = theta > 0 ? static_cast<float>(1.0 / theta) : FLT_MAX;
     Moments mo{t.nd_com.as<float4>(), t.nd_comlo.as<float4>(), t.nd_q0.as<float4>(), t.nd_q1.as<float4>()};
     k_leaf_moments<<<grid_for(static_cast<long long>(K), 128), 128, 0, s>>>(
-        t.leaf_order.as<uint32_t>(), static_cast<uint32_t>(K), static_cast<uint32_t>(T), t.nd_range.as<uint4>(),
-        t.nd_geo.as<float4>(), e.bodies(e.cur), mo, inv_theta, e.err_word());
+        t.leaf_order.as<uint32_t>(), Kc, Kdev, Tc, Tdev, t.nd_range.as<uint4>(), t.nd_geo.as<float4>(), e.bodies(e.cur),
+        mo, inv_theta, e.err_word());
     LG_LAUNCHED();
-    e.launches += 6;
+    e.launches += 4;
     const int cb = std::max(1, std::min(4 * e.sms, grid_for(static_cast<long long>(T), 128)));
-    for (int d = t.max_depth - 1; d >= 0; --d) {
-        k_combine_level<<<cb, 128, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, static_cast<uint32_t>(T),
-                                           t.nd_range.as<uint4>(), t.nd_geo.as<float4>(), mo, inv_theta, e.err_word());
+    for (int d = depth - 1; d >= 0; --d) {
+        k_combine_level<<<cb, 128, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, Tc, Tdev, t.nd_range.as<uint4>(),
+                                           t.nd_geo.as<float4>(), mo, inv_theta, e.err_word());
         LG_LAUNCHED();
         ++e.launches;
     }
 }
+
+// After a synchronising point: true if the tree built with guessed sizes is valid (no key restart
+// was missed, leaves, nodes and depth within what was launched). Otherwise records the exact need
+// so that the caller's rebuild takes the exact path.
+bool tree_verify(Engine& e, const unsigned* counts_host) {
+    TreeState& t = *e.tree;
+    if (!t.speculative) return true;
+    const unsigned R = counts_host[0], K = counts_host[1], T = counts_host[2];
+    const int depth = static_cast<int>(counts_host[4]);
+    const bool ok = (t.restarted || R == 0) && K <= t.K && T <= t.T && depth <= t.max_depth;
+    if (!ok) {
+        if (!t.restarted && R > 0) t.restart_mode = true;
+        t.have_guess = false;  // next build reads exact sizes
+    }
+    return ok;
+}
+
+const unsigned* tree_counts_device(Engine& e) { return e.tree->counts.as<unsigned>(); }
+void tree_reset_guess(Engine& e) {
+    e.tree->have_guess = false;
+    e.tree->restart_mode = false;
+}
+double tree_theta(const Engine& e) { return e.tree->theta; }
 
 TreeView tree_view(Engine& e) {
     TreeState& t = *e.tree;
@@ -1272,13 +1341,14 @@ TreeView tree_view(Engine& e) {
     v.grp_range = t.grp_range.as<uint2>();
     v.grp_box = t.grp_box.as<float4>();
     v.ngroups = t.counts.as<unsigned>() + 3;
-    v.T = t.T;
+    v.T = t.T;  // capacity the build was launched with (>= the node count)
     return v;
 }
 
 void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth) {
     TreeState& t = *e.tree;
     if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    e.ensure_tree_valid();
     LG_CK(cudaMemcpyAsync(e.pinned_small, t.counts.as<unsigned>(), 32, cudaMemcpyDeviceToHost, e.stream));
     LG_CK(cudaStreamSynchronize(e.stream));
     if (nodes) *nodes = e.pinned_small[2];
@@ -1293,6 +1363,7 @@ void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* 
 void tree_keys(Engine& e, uint64_t* keys, size_t n) {
     TreeState& t = *e.tree;
     if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
+    e.ensure_tree_valid();
     if (n < static_cast<size_t>(e.n)) fail(kArg, "tree_keys: output holds fewer than n keys");
     const size_t N = static_cast<size_t>(e.n);
     LG_CK(cudaMemcpyAsync(keys, t.skey.as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));

@@ -276,3 +276,36 @@ def test_one_million_body_tree_force_call(be):
     t = be.times()
     print(f"1M tree: force {t.force_ms:.2f} ms (sort {t.sort_ms:.2f}, build {t.build_ms:.2f}, walk {t.walk_ms:.2f}),"
           f" {t.interactions / n:.1f} interactions/body")
+
+
+def test_sync_free_build_recovers_from_a_missed_key_restart(be):
+    """Steps after the first build size the tree from the previous one and assume no key
+    restart; a drift that makes 40 bodies coincide must be caught and rebuilt exactly."""
+    b = S.cube(2000, 5)
+    b.vx[:] = 0
+    b.vy[:] = 0
+    b.vz[:] = 0
+    rng = np.random.Generator(np.random.PCG64(3))
+    v = rng.integers(-64, 64, (40, 3)).astype(np.float64) / 1024.0  # dyadic: x + v lands exactly on p0
+    p0 = np.array([0.5, 0.25, -0.125])
+    b.x[:40] = p0[0] - v[:, 0]
+    b.y[:40] = p0[1] - v[:, 1]
+    b.z[:40] = p0[2] - v[:, 2]
+    b.vx[:40] = v[:, 0]
+    b.vy[:40] = v[:, 1]
+    b.vz[:40] = v[:, 2]
+    p = params(1, 0.05, 0.0)
+    be.upload(b)
+    be.compute_forces(p, True)
+    be.drift(1.0)
+    be.compute_forces(p, True)
+    n = len(b)
+    assert be.times().interactions == n * (n - 1)
+    out = be.download()
+    pos = be.pos64()
+    assert np.all(pos[0, out.id < 40] == p0[0])
+    cnt = be.tree_counts()
+    assert cnt["max_depth"] >= 21
+    # Same forces as a fresh build from the same positions.
+    ref = O.direct_fp64(out, 1.0, 0.05)
+    assert rel_rms(be.accel()[:3], ref[:3]) <= 1e-5
