@@ -51,7 +51,7 @@ inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) 
 constexpr int RADIX = 256;
 constexpr int PASSES = 8;
 constexpr int SORT_BS = 256;
-constexpr int SORT_IPT = 16;
+constexpr int SORT_IPT = 8;
 constexpr int SORT_TILE = SORT_BS * SORT_IPT;
 constexpr unsigned FLAG_AGG = 1u << 30, FLAG_INC = 2u << 30, VAL_MASK = (1u << 30) - 1;
 
@@ -269,7 +269,10 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
                                                        unsigned* __restrict__ lookback, SortCtl* ctl,
                                                        unsigned* err) {
     __shared__ unsigned warp_hist[SORT_BS / 32][RADIX];
-    __shared__ unsigned gbase[RADIX];
+    __shared__ unsigned gbase[RADIX];       // global start of each digit for this tile
+    __shared__ unsigned tstart[RADIX];      // inclusive scan of the tile's digit counts
+    __shared__ uint64_t stage_k[SORT_TILE]; // the tile in digit order
+    __shared__ uint32_t stage_v[SORT_TILE];
     __shared__ unsigned tile_s, sel_s;
     if (ctl->skip[pass]) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -286,13 +289,16 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
     uint64_t* dst_k = sel_s ? kA : kB;
     uint32_t* dst_v = sel_s ? vA : vB;
     const int shift = 8 * pass;
-    const int wbase = tile * SORT_TILE + w * (32 * SORT_IPT);
+    const int tile0 = tile * SORT_TILE;
+    const int wbase = tile0 + w * (32 * SORT_IPT);
+    const int tile_n = min(SORT_TILE, n - tile0);
 
     uint64_t key[SORT_IPT];
     uint32_t val[SORT_IPT];
     unsigned rank[SORT_IPT];
     int dig[SORT_IPT];
     const unsigned lt = (1u << lane) - 1u;
+    // Stable rank inside the tile: keys in index order (warp, round, lane).
 #pragma unroll
     for (int r = 0; r < SORT_IPT; ++r) {
         const int i = wbase + r * 32 + lane;
@@ -311,9 +317,9 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
         rank[r] = basev + before;
     }
     __syncthreads();
-    // Per digit: offsets of each warp inside the tile, and the tile's count.
-    unsigned tile_count;
     {
+        // Per digit (thread d): offsets of the warps inside the digit, the tile's count, then the
+        // decoupled look-back across tiles for the digit's global start.
         const int d = tid;
         unsigned run = 0;
 #pragma unroll
@@ -322,7 +328,7 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
             warp_hist[u][d] = run;
             run += c;
         }
-        tile_count = run;
+        const unsigned tile_count = run;
         volatile unsigned* lb = lookback + static_cast<size_t>(tile) * RADIX;
         unsigned prefix = 0;
         if (tile == 0) {
@@ -350,17 +356,38 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
             lb[d] = FLAG_INC | ((prefix + tile_count) & VAL_MASK);
         }
         gbase[d] = offsets[pass * RADIX + d] + prefix;
+        // Exclusive scan of the tile's digit counts (Hillis-Steele over 256 threads).
+        tstart[d] = tile_count;
     }
     __syncthreads();
+    for (int o = 1; o < RADIX; o <<= 1) {
+        const unsigned t = tid >= o ? tstart[tid - o] : 0u;
+        __syncthreads();
+        tstart[tid] += t;
+        __syncthreads();
+    }
+    // tstart now holds the inclusive scan: digit d starts at tstart[d - 1] (0 for d = 0).
+    // Stage the tile in digit order (tile-local position = digit start + rank within the digit).
 #pragma unroll
     for (int r = 0; r < SORT_IPT; ++r) {
         const int i = wbase + r * 32 + lane;
         if (i < n) {
             const int d = dig[r];
-            const unsigned pos = gbase[d] + warp_hist[w][d] + rank[r];
-            dst_k[pos] = key[r];
-            dst_v[pos] = val[r];
+            const unsigned excl = (d > 0 ? tstart[d - 1] : 0u);
+            const unsigned pos = excl + warp_hist[w][d] + rank[r];
+            stage_k[pos] = key[r];
+            stage_v[pos] = val[r];
         }
+    }
+    __syncthreads();
+    // Write out: consecutive staged entries of one digit go to consecutive global addresses.
+    for (int p = tid; p < tile_n; p += SORT_BS) {
+        const uint64_t k = stage_k[p];
+        const int d = static_cast<int>((k >> shift) & 255);
+        const unsigned excl = (d > 0 ? tstart[d - 1] : 0u);
+        const unsigned gpos = gbase[d] + (p - excl);
+        dst_k[gpos] = k;
+        dst_v[gpos] = stage_v[p];
     }
     // The last tile to finish flips the buffer selector (every tile has read it by then).
     __syncthreads();
@@ -959,51 +986,87 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
 
 // Internal nodes of one depth: combine the children (already final) in index order, FP64, the
 // parallel-axis theorem for the traceless quadrupole (src/cpu_backend.cpp:642-663).
+// Eight lanes per node (four nodes per warp): lane j forms child j's terms, then every lane of the
+// node replays the reference's sequential child-order sums from the shuffled terms, so the result
+// is the sequential one bit for bit while the per-child FP64 work runs in parallel.
+__device__ __forceinline__ double shfl8(double v, int src_lane) { return __shfl_sync(0xffffffffu, v, src_lane); }
+
 __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth,
                                 uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
                                 const float4* __restrict__ nd_geo, Moments mo, float inv_theta, unsigned* err) {
     const uint32_t T = eff(Tdev, Tcap);
     const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
-    for (unsigned k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
-        const uint32_t p = dep_nodes[k];
-        if (p >= T) {
-            atomicOr(err, kErrNodeOverflow);
-            continue;
+    const int lane = threadIdx.x & 31, sub = lane >> 3, j = lane & 7, base_lane = lane & ~7;
+    const unsigned warps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (unsigned k0 = lo + 4 * wid; k0 < hi; k0 += 4 * warps) {
+        const unsigned k = k0 + sub;
+        bool valid = k < hi;
+        uint32_t p = valid ? dep_nodes[k] : 0u;
+        uint4 r = make_uint4(0, 0, 0, 0);
+        if (valid) {
+            if (p >= T) {
+                if (j == 0) atomicOr(err, kErrNodeOverflow);
+                valid = false;
+            } else {
+                r = nd_range[p];
+                if (r.w == 0 || r.w > 8 || r.z + r.w > T) {
+                    if (j == 0) atomicOr(err, kErrNodeOverflow);
+                    valid = false;
+                }
+            }
         }
-        const uint4 r = nd_range[p];
-        if (r.w == 0 || r.z + r.w > T) {
-            atomicOr(err, kErrNodeOverflow);
-            continue;
+        const int nch = valid ? static_cast<int>(r.w) : 0;
+        const bool mine = j < nch;
+        float4 cm = make_float4(0, 0, 0, 0), a = cm, e = cm;
+        if (mine) {
+            const uint32_t c = r.z + j;
+            cm = mo.com[c];
+            a = mo.q0[c];
+            e = mo.q1[c];
         }
-        const float4 g = nd_geo[p];
+        const double m = cm.w;
+        const double mx = DMUL(m, static_cast<double>(cm.x)), my = DMUL(m, static_cast<double>(cm.y)),
+                     mz = DMUL(m, static_cast<double>(cm.z));
         double M = 0, sx = 0, sy = 0, sz = 0;
-        for (uint32_t c = r.z; c < r.z + r.w; ++c) {
-            const float4 cm = mo.com[c];
-            const double m = cm.w;
-            M = DADD(M, m);
-            sx = DADD(sx, DMUL(m, static_cast<double>(cm.x)));
-            sy = DADD(sy, DMUL(m, static_cast<double>(cm.y)));
-            sz = DADD(sz, DMUL(m, static_cast<double>(cm.z)));
+        for (int q = 0; q < 8; ++q) {
+            const double tm = shfl8(m, base_lane + q), tx = shfl8(mx, base_lane + q), ty = shfl8(my, base_lane + q),
+                         tz = shfl8(mz, base_lane + q);
+            if (q < nch) {
+                M = DADD(M, tm);
+                sx = DADD(sx, tx);
+                sy = DADD(sy, ty);
+                sz = DADD(sz, tz);
+            }
         }
+        const float4 g = valid ? nd_geo[p] : make_float4(0, 0, 0, 0);
         const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
                      cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
+        const double dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
+                     dz = DSUB(static_cast<double>(cm.z), cz);
+        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+        const double m3 = DMUL(m, 3.0);
+        const double txx = DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
+        const double tyy = DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
+        const double tzz = DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
+        const double txy = DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy));
+        const double txz = DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz));
+        const double tyz = DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz));
         double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
-        for (uint32_t c = r.z; c < r.z + r.w; ++c) {
-            const float4 cm = mo.com[c];
-            const float4 a = mo.q0[c];
-            const float4 e = mo.q1[c];
-            const double m = cm.w, dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
-                         dz = DSUB(static_cast<double>(cm.z), cz);
-            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
-            const double m3 = DMUL(m, 3.0);
-            qxx = DADD(qxx, DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2))));
-            qyy = DADD(qyy, DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2))));
-            qzz = DADD(qzz, DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2))));
-            qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy)));
-            qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz)));
-            qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz)));
+        for (int q = 0; q < 8; ++q) {
+            const int sl = base_lane + q;
+            const double vxx = shfl8(txx, sl), vxy = shfl8(txy, sl), vxz = shfl8(txz, sl), vyy = shfl8(tyy, sl),
+                         vyz = shfl8(tyz, sl), vzz = shfl8(tzz, sl);
+            if (q < nch) {
+                qxx = DADD(qxx, vxx);
+                qyy = DADD(qyy, vyy);
+                qzz = DADD(qzz, vzz);
+                qxy = DADD(qxy, vxy);
+                qxz = DADD(qxz, vxz);
+                qyz = DADD(qyz, vyz);
+            }
         }
-        store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+        if (valid && j == 0) store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
     }
 }
 
