@@ -203,6 +203,117 @@ def adjoint_leg(L, local, steps=1000, every=32, n=65536):
                            "m": float(np.linalg.norm(gm))}}
 
 
+def fp64_direct_error(pos, m, acc, eps, count=64, seed=7):
+    """Median and maximum per-body relative error of acc (n, 3) against an FP64 direct sum over
+    all bodies (positions pos (n, 3), masses m), for a seeded sample of bodies."""
+    n = len(m)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pick = rng.choice(n, size=min(count, n), replace=False)
+    errs = []
+    for s in range(0, len(pick), 16):
+        idx = pick[s:s + 16]
+        d = pos[None, :, :] - pos[idx][:, None, :]
+        r2 = (d * d).sum(-1) + eps * eps
+        r2[np.arange(len(idx)), idx] = np.inf
+        ref = (d * (m[None, :] * r2 ** -1.5)[..., None]).sum(1)
+        errs.extend((np.linalg.norm(acc[idx] - ref, axis=1) / np.linalg.norm(ref, axis=1)).tolist())
+    return float(np.median(errs)), float(np.max(errs))
+
+
+def ensemble_leg(L, local, steps=200, seq_steps=10, count=512):
+    """Batched ensemble at the configuration-3 shape: 512 Plummer clusters (seeds 100-611), N
+    log-uniform in [1024, 131072], eps = 0.01 (N/16384)^(-1/3), direct for N <= 8192 else tree
+    theta 0.5, dt 1e-3, `steps` KDK steps as one CUDA graph (after the autotuner). Compared with
+    the same systems run one at a time through the plain engine API (upload, then KDK steps with
+    compute_forces), timed over `seq_steps` steps per system. Throughput in bodies x steps / s."""
+    from lettuce_simulate_physics_gb300 import scenarios as S
+    from lettuce_simulate_physics_gb300.ensemble import Ensemble
+    b, counts, eps, theta, methods = S.ensemble(count)
+    n = int(counts.sum())
+    off = np.concatenate([[0], np.cumsum(counts.astype(np.int64))])
+    dt = 1e-3
+    en = Ensemble(local)
+    en.upload(b, counts, eps, theta, methods)
+    t0 = time.perf_counter()
+    tun = en.tune()
+    tune_s = time.perf_counter() - t0
+    e0, _, _ = en.energy()
+    # Force accuracy at t = 0 on four systems (smallest/largest direct and tree) vs FP64 direct.
+    acc = en.accel()
+    got = en.download()
+    picks = []
+    for meth in (0, 1):
+        idx = np.flatnonzero(methods == meth)
+        if len(idx):
+            picks += [int(idx[np.argmin(counts[idx])]), int(idx[np.argmax(counts[idx])])]
+    ferr = {}
+    for k in picks:
+        lo, hi = int(off[k]), int(off[k + 1])
+        order = np.argsort(got.id[lo:hi])
+        pos = np.stack([b.x[lo:hi], b.y[lo:hi], b.z[lo:hi]], 1).astype(np.float64)
+        a = acc[:3, lo:hi].T[order].astype(np.float64)
+        med, mx = fp64_direct_error(pos, b.m[lo:hi].astype(np.float64), a, float(eps[k]))
+        ferr[f"sys{k}_N{hi - lo}_{'tree' if methods[k] else 'direct'}"] = {"median": med, "max": mx}
+    # Batched: `steps` steps as one CUDA graph. The first run captures it (its energy change over
+    # the configured 200 steps from t = 0 is the reported error); the timed run replays it.
+    t0 = time.perf_counter()
+    en.run(dt, steps, use_graph=True)
+    first_wall = time.perf_counter() - t0
+    e1, _, _ = en.energy()
+    rel = np.abs((e1 - e0) / e0)
+    t0 = time.perf_counter()
+    en.run(dt, steps, use_graph=True)
+    wall = time.perf_counter() - t0
+    st = en.stats()
+    en.close()
+    batched_dev = n * steps / (st.run_ms * 1e-3)
+    batched_wall = n * steps / wall
+    # One at a time through the plain API.
+    be = L.CudaBackend(local)
+    seq_dev_ms = 0.0
+    seq_wall_s = 0.0
+    for k in range(len(counts)):
+        lo, hi = int(off[k]), int(off[k + 1])
+        sb = L.Bodies(b.x[lo:hi], b.y[lo:hi], b.z[lo:hi], b.vx[lo:hi], b.vy[lo:hi], b.vz[lo:hi], b.m[lo:hi],
+                      b.id[lo:hi])
+        p = L.ForceParams(G=1.0, eps=float(eps[k]), theta=float(theta[k]),
+                          method=L.ForceMethod.tree if methods[k] else L.ForceMethod.direct)
+        be.upload(sb)
+        be.compute_forces(p, False)
+        be.synchronize()
+        t0 = time.perf_counter()
+        be.event_record(8)
+        for _ in range(seq_steps):
+            be.kick(0.5 * dt)
+            be.drift(dt)
+            be.compute_forces(p, False)
+            be.kick(0.5 * dt)
+        be.event_record(9)
+        be.synchronize()
+        seq_wall_s += time.perf_counter() - t0
+        seq_dev_ms += be.event_elapsed(8, 9)
+    be.close()
+    seq_dev = n * seq_steps / (seq_dev_ms * 1e-3)
+    seq_wall = n * seq_steps / seq_wall_s
+    return {
+        "systems": int(len(counts)), "n_total": n, "n_tree_systems": int((methods == 1).sum()),
+        "n_direct_systems": int((methods == 0).sum()), "steps": steps, "dt": dt,
+        "tuning": {"direct_ipt": list(tun.direct_ipt), "walk_group": tun.walk_group, "tune_s": round(tune_s, 2)},
+        "batched": {"run_ms": round(st.run_ms, 3), "wall_s": round(wall, 4), "used_graph": st.used_graph,
+                    "recoveries": st.recoveries, "launches_per_step": st.launches_per_step,
+                    "bodies_steps_per_s": batched_dev, "bodies_steps_per_s_wall": batched_wall,
+                    "captures": st.captures, "first_run_wall_s": round(first_wall, 4)},
+        "sequential": {"steps_per_system": seq_steps, "device_ms": round(seq_dev_ms, 3),
+                       "wall_s": round(seq_wall_s, 4), "bodies_steps_per_s": seq_dev,
+                       "bodies_steps_per_s_wall": seq_wall},
+        "batched_over_sequential": round(batched_wall / seq_wall, 3),
+        "batched_over_sequential_device": round(batched_dev / seq_dev, 3),
+        "energy_rel_error": {"median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
+                             "max": float(np.max(rel)), "steps": steps},
+        "force_error_vs_fp64_t0": ferr,
+    }
+
+
 def read_profile_traffic(workload):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -347,6 +458,10 @@ def run_gb300(args, w, world, rank, local, dist):
     if rank == 0 and not args.no_adjoint:
         adj = adjoint_leg(L, local, steps=args.adjoint_steps)
 
+    ens = None
+    if rank == 0 and not args.no_ensemble:
+        ens = ensemble_leg(L, local, steps=args.ensemble_steps)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
@@ -367,6 +482,7 @@ def run_gb300(args, w, world, rank, local, dist):
                          "flops_per_unit": {"body_pair": 20, "cell_term": 65}},
             "cpu_baseline": cpu,
             "adjoint": adj,
+            "ensemble": ens,
             "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": int(launches),
@@ -389,6 +505,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--adjoint-steps", type=int, default=1000, help="KDK steps of the adjoint leg")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--ensemble-steps", type=int, default=200, help="KDK steps of the ensemble leg")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     world, rank, local, dist = dist_setup()

@@ -176,6 +176,59 @@ lg_status lg_adjoint_backward(lg_engine* e, const double* target_x, const double
                               double* loss, double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz,
                               double* gm);
 
+/* ---- Batched ensembles (no reference counterpart) ----------------------------------------------
+ * Many independent systems of uneven N advanced together: every force phase is one launch pipeline
+ * over all systems (a batched direct-sum launch per i-bodies-per-thread class, one forest tree for
+ * the tree systems: one sort, one build, one walk), and a run of steps can be captured as one CUDA
+ * graph. Each system has its own softening, opening angle and method; G and dt are shared. */
+typedef struct lg_ensemble lg_ensemble;
+
+typedef struct {
+    double run_ms;          /* device time of the last lg_ensemble_run (CUDA events) */
+    int steps;              /* steps of the last run */
+    int used_graph;         /* 1 if the last run replayed a captured graph */
+    int captures;           /* graphs captured so far */
+    int recoveries;         /* runs redone with exact tree sizes after a sync-free build missed */
+    int nsys, nsys_tree, nsys_direct;
+    size_t n, n_tree, n_direct;
+    unsigned long long launches_per_step; /* kernels launched per step (both streams) */
+    unsigned long long last_interactions; /* body pairs + cell terms of the last force phase */
+} lg_ensemble_stats;
+
+/* Tuning: i-bodies per thread of the batched direct kernel for systems with N < 2048, N < 4096
+ * and larger (classes 0-2), and the walk group size of the forest tree. */
+typedef struct {
+    int direct_ipt[3];
+    int walk_group;
+    int tuned;              /* 1 after lg_ensemble_tune measured or loaded them */
+} lg_ensemble_tuning;
+
+lg_status lg_ensemble_create(int device, lg_ensemble** out);
+lg_status lg_ensemble_destroy(lg_ensemble* en);
+/* Systems back to back in the input arrays: system s has counts[s] bodies, softening eps[s] > 0,
+ * opening angle theta[s] (tree systems) and method[s] (LG_DIRECT or LG_TREE). */
+lg_status lg_ensemble_upload(lg_ensemble* en, size_t nsys, const uint32_t* counts, const double* eps,
+                             const double* theta, const int* method, double G, const float* x, const float* y,
+                             const float* z, const float* vx, const float* vy, const float* vz, const float* m,
+                             const uint32_t* id);
+/* `steps` kick-drift-kick steps of size dt; use_graph != 0 captures them as one CUDA graph (reused
+ * by later runs with the same steps and dt). Synchronises. */
+lg_status lg_ensemble_run(lg_ensemble* en, double dt, int steps, int use_graph);
+/* Per-system total energy (kinetic + potential, FP64; input system order) at the current state;
+ * evaluates forces with potentials. ke / pe may be NULL. */
+lg_status lg_ensemble_energy(lg_ensemble* en, double* energy, double* ke, double* pe);
+/* Bodies in input system order; within a system, in the engine's current order (ids identify). */
+lg_status lg_ensemble_download(lg_ensemble* en, float* x, float* y, float* z, float* vx, float* vy, float* vz,
+                               float* m, uint32_t* id);
+/* Accelerations and potentials of the last force phase, in lg_ensemble_download's order. */
+lg_status lg_ensemble_read_accel(lg_ensemble* en, float* ax, float* ay, float* az, float* pot);
+/* Times the candidates on the resident ensemble and keeps the fastest; with a cache file named by
+ * LETTUCE_GB300_TUNE_CACHE, an entry for this device is loaded instead (and new results saved). */
+lg_status lg_ensemble_tune(lg_ensemble* en);
+lg_status lg_ensemble_get_tuning(lg_ensemble* en, lg_ensemble_tuning* out);
+lg_status lg_ensemble_set_tuning(lg_ensemble* en, const lg_ensemble_tuning* t);
+lg_status lg_ensemble_get_stats(lg_ensemble* en, lg_ensemble_stats* out);
+
 /* Direct-summation forces with no device allocation. No counterpart in the reference: it is for
  * callers that cannot allocate device memory when they need forces, such as a code that owns all
  * device memory through its own fixed arena, or a stepping loop that must avoid cudaMalloc's

@@ -109,6 +109,17 @@ class _CMem(C.Structure):
     _fields_ = [("device", C.c_uint64), ("host", C.c_uint64)]
 
 
+class _CEnsStats(C.Structure):
+    _fields_ = [("run_ms", C.c_double), ("steps", C.c_int), ("used_graph", C.c_int), ("captures", C.c_int),
+                ("recoveries", C.c_int), ("nsys", C.c_int), ("nsys_tree", C.c_int), ("nsys_direct", C.c_int),
+                ("n", C.c_size_t), ("n_tree", C.c_size_t), ("n_direct", C.c_size_t),
+                ("launches_per_step", C.c_ulonglong), ("last_interactions", C.c_ulonglong)]
+
+
+class _CEnsTuning(C.Structure):
+    _fields_ = [("direct_ipt", C.c_int * 3), ("walk_group", C.c_int), ("tuned", C.c_int)]
+
+
 _f = C.POINTER(C.c_float)
 _u = C.POINTER(C.c_uint32)
 _d = C.POINTER(C.c_double)
@@ -168,6 +179,18 @@ def _lib() -> C.CDLL:
         "lg_adjoint_forward": (st, [vp, C.POINTER(_CForceParams), C.c_double, C.c_int, C.c_int]),
         "lg_adjoint_backward": (st, [vp, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d]),
         "lg_host_free": (st, [vp]),
+        "lg_ensemble_create": (st, [C.c_int, C.POINTER(vp)]),
+        "lg_ensemble_destroy": (st, [vp]),
+        "lg_ensemble_upload": (st, [vp, C.c_size_t, _u, _d, _d, C.POINTER(C.c_int), C.c_double,
+                                    _f, _f, _f, _f, _f, _f, _f, _u]),
+        "lg_ensemble_run": (st, [vp, C.c_double, C.c_int, C.c_int]),
+        "lg_ensemble_energy": (st, [vp, _d, _d, _d]),
+        "lg_ensemble_download": (st, [vp, _f, _f, _f, _f, _f, _f, _f, _u]),
+        "lg_ensemble_read_accel": (st, [vp, _f, _f, _f, _f]),
+        "lg_ensemble_tune": (st, [vp]),
+        "lg_ensemble_get_tuning": (st, [vp, C.POINTER(_CEnsTuning)]),
+        "lg_ensemble_set_tuning": (st, [vp, C.POINTER(_CEnsTuning)]),
+        "lg_ensemble_get_stats": (st, [vp, C.POINTER(_CEnsStats)]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)

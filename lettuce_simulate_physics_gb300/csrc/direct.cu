@@ -34,16 +34,17 @@ struct alignas(16) DirectSmem {
     uint64_t bar[2];
 };
 
+// One block's work: i-bodies [base, base + DBS * IPT) clipped to iend, against j-bodies [j0, j1).
+// write_final: out[i] = G-scaled sums; otherwise out[i] = unscaled partial sums (out points at the
+// slice's row).
 template <int IPT, bool POT, bool EPS0>
-__global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
-                                                int jslice, float G, float e2, float4* __restrict__ out, int write_final,
-                                                unsigned* err) {
-    __shared__ DirectSmem sm;
+__device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __restrict__ hm,
+                                             const float4* __restrict__ lo, int base, int iend, int j0, int j1,
+                                             float G, float e2, float4* __restrict__ out, bool write_final,
+                                             unsigned* err) {
     const int tid = threadIdx.x;
-    const int base = blockIdx.x * (DBS * IPT);
-    const int j0 = blockIdx.y * jslice;
-    const int j1 = min(n, j0 + jslice);
     const int ntiles = (j1 - j0 + TILE - 1) / TILE;
+    const int n = iend;
 
     // Block origin: the first i-body of the block.
     const float4 oh = hm[base];
@@ -183,9 +184,29 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
         if (write_final)
             out[i] = make_float4(G * (sx[u] - cx[u]), G * (sy[u] - cy[u]), G * (sz[u] - cz[u]), POT ? -G * p : 0.f);
         else
-            out[static_cast<size_t>(blockIdx.y) * n + i] =
-                make_float4(sx[u] - cx[u], sy[u] - cy[u], sz[u] - cz[u], POT ? p : 0.f);
+            out[i] = make_float4(sx[u] - cx[u], sy[u] - cy[u], sz[u] - cz[u], POT ? p : 0.f);
     }
+}
+
+template <int IPT, bool POT, bool EPS0>
+__global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
+                                                int jslice, float G, float e2, float4* __restrict__ out, int write_final,
+                                                unsigned* err) {
+    __shared__ DirectSmem sm;
+    const int j0 = blockIdx.y * jslice;
+    direct_block<IPT, POT, EPS0>(sm, hm, lo, blockIdx.x * (DBS * IPT), n, j0, min(n, j0 + jslice), G, e2,
+                                 write_final ? out : out + static_cast<size_t>(blockIdx.y) * n, write_final != 0, err);
+}
+
+// Many independent systems in one launch: block b takes work item b (an i-tile of one system
+// against all of that system's bodies), with the system's own softening.
+template <int IPT, bool POT, bool EPS0>
+__global__ void __launch_bounds__(DBS) k_direct_batch(const float4* __restrict__ hm, const float4* __restrict__ lo,
+                                                      const DirectWork* __restrict__ work, float G,
+                                                      float4* __restrict__ acc, unsigned* err) {
+    __shared__ DirectSmem sm;
+    const DirectWork w = work[blockIdx.x];
+    direct_block<IPT, POT, EPS0>(sm, hm, lo, w.base, w.iend, w.j0, w.j1, G, w.e2, acc, true, err);
 }
 
 // Sums the split-j partials in slice order (Kahan) and scales by G.
@@ -263,6 +284,34 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
     if (!final_out) {
         k_direct_reduce<<<(n + 255) / 256, 256, 0, s>>>(partial, n, slices, G, acc);
         LG_LAUNCHED();
+    }
+}
+
+namespace {
+template <int IPT>
+void launch_batch_ipt(const BodyArrays b, const DirectWork* work, int nwork, float G, bool pot, bool eps0, float4* acc,
+                      unsigned* err, cudaStream_t s) {
+    if (pot) {
+        if (eps0) k_direct_batch<IPT, true, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        else k_direct_batch<IPT, true, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+    } else {
+        if (eps0) k_direct_batch<IPT, false, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        else k_direct_batch<IPT, false, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+    }
+    LG_LAUNCHED();
+}
+}  // namespace
+
+int direct_block_bodies(int ipt) { return DBS * ipt; }
+
+void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, float G, bool potential,
+                         bool eps0, float4* acc, unsigned* err, cudaStream_t s) {
+    if (nwork <= 0) return;
+    switch (ipt) {
+        case 1: launch_batch_ipt<1>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+        case 2: launch_batch_ipt<2>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+        case 8: launch_batch_ipt<8>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+        default: launch_batch_ipt<4>(b, work, nwork, G, potential, eps0, acc, err, s); break;
     }
 }
 

@@ -112,6 +112,17 @@ bool tree_verify(Engine& e, const unsigned* counts_host);
 const unsigned* tree_counts_device(Engine& e);
 void tree_reset_guess(Engine& e);
 double tree_theta(const Engine& e);
+// Forest mode (ensembles): the tree covers bodies [0, n_tree) of nsys systems; sys (per body),
+// sys_off (nsys + 1 body offsets) and inv_theta_sys (per system) are device arrays the caller
+// keeps alive. n_tree < 0 restores the single-system tree.
+void tree_set_forest(Engine& e, int n_tree, int nsys, const uint32_t* sys, const uint32_t* sys_off,
+                     const float* inv_theta_sys);
+// True when the next build takes no host read (sizes guessed from the previous build).
+bool tree_sync_free_ready(const Engine& e);
+// Changes whenever a build may have reallocated tree buffers (captured graphs must be redone).
+uint64_t tree_generation(const Engine& e);
+// Device-side form of tree_verify for a sync-free build: ORs 1 into *sticky on a miss.
+void tree_check_async(Engine& e, unsigned* sticky);
 void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* max_depth);
 void tree_keys(Engine& e, uint64_t* keys, size_t n);
 void tree_nodes(Engine& e, uint32_t* lohi_first_nchild, float* moments11, float* geo4, size_t nodes);
@@ -119,7 +130,9 @@ void tree_groups(Engine& e, float* box6, uint32_t* lohi, size_t groups);
 lg_memory_estimate memory_need(uint64_t n, int method);
 const void* probe_kernel();
 // walk.cu
-void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0);
+// sys/e2_sys: forest walk (per-body system, per-system squared softening); nullptr for one tree.
+void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys = nullptr,
+               const float* e2_sys = nullptr);
 // adjoint.cu
 std::unique_ptr<AdjointState, void (*)(AdjointState*)> make_adjoint_state();
 void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every);

@@ -71,6 +71,27 @@ __global__ void k_drift(BodyArrays b, double dt, int n) {
     store_hilo(b, i, px, py, pz, b.m[i]);
 }
 
+// Ensemble step opening: v += a (dt/2), then x += v dt -- the kick and drift kernels' arithmetic in
+// one pass over the bodies.
+__global__ void k_kick_drift(BodyArrays b, const float4* __restrict__ acc, float hdt, double dt, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = acc[i];
+    const float vx = __fmaf_rn(a.x, hdt, b.vx[i]);
+    const float vy = __fmaf_rn(a.y, hdt, b.vy[i]);
+    const float vz = __fmaf_rn(a.z, hdt, b.vz[i]);
+    b.vx[i] = vx;
+    b.vy[i] = vy;
+    b.vz[i] = vz;
+    const double px = __fma_rn(static_cast<double>(vx), dt, b.x[i]);
+    const double py = __fma_rn(static_cast<double>(vy), dt, b.y[i]);
+    const double pz = __fma_rn(static_cast<double>(vz), dt, b.z[i]);
+    b.x[i] = px;
+    b.y[i] = py;
+    b.z[i] = pz;
+    store_hilo(b, i, px, py, pz, b.m[i]);
+}
+
 constexpr int NDIAG = 12;
 
 // Block-level FP64 sum of NDIAG values in a fixed order (warp shuffles, then warps in order).
@@ -139,6 +160,26 @@ __global__ void k_diag(const BodyArrays b, const float4* __restrict__ acc, int n
 }
 
 // Bounding box of the FP64 positions: out6 = min xyz, max xyz.
+// Per-system energies of an ensemble: block s sums kinetic energy (1/2) m v^2 and potential
+// energy (1/2) m phi over the body range [off[s], off[s + 1]) in FP64, in a fixed order.
+__global__ void k_sys_energy(const BodyArrays b, const float4* __restrict__ acc, const uint32_t* __restrict__ off,
+                             double* __restrict__ out) {
+    __shared__ double sh[(BS / 32) * NDIAG];
+    const uint32_t lo = off[blockIdx.x], hi = off[blockIdx.x + 1];
+    double v[NDIAG] = {};
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += BS) {
+        const double m = b.m[i];
+        const double vx = b.vx[i], vy = b.vy[i], vz = b.vz[i];
+        v[0] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        v[1] += 0.5 * m * static_cast<double>(acc[i].w);
+    }
+    block_sum(v, sh);
+    if (threadIdx.x == 0) {
+        out[2 * blockIdx.x] = v[0];
+        out[2 * blockIdx.x + 1] = v[1];
+    }
+}
+
 __global__ void k_bounds(const BodyArrays b, int n, double* partial, unsigned* ticket, double* out6) {
     __shared__ double sh[6][BS / 32];
     __shared__ bool last;
@@ -311,6 +352,19 @@ void launch_kick(BodyArrays b, const float4* acc, float dt, int n, cudaStream_t 
 void launch_drift(BodyArrays b, double dt, int n, cudaStream_t s) {
     if (n <= 0) return;
     k_drift<<<grid_for(n, BS), BS, 0, s>>>(b, dt, n);
+    LG_LAUNCHED();
+}
+
+void launch_kick_drift(BodyArrays b, const float4* acc, float hdt, double dt, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_kick_drift<<<grid_for(n, BS), BS, 0, s>>>(b, acc, hdt, dt, n);
+    LG_LAUNCHED();
+}
+
+void launch_sys_energy(const BodyArrays b, const float4* acc, const uint32_t* off, int nsys, double* out,
+                       cudaStream_t s) {
+    if (nsys <= 0) return;
+    k_sys_energy<<<nsys, BS, 0, s>>>(b, acc, off, out);
     LG_LAUNCHED();
 }
 

@@ -44,6 +44,11 @@ void launch_widen(const float* x, const float* y, const float* z, const float* m
 void launch_round_pos(const BodyArrays b, float* x, float* y, float* z, int n, cudaStream_t s);
 void launch_kick(BodyArrays b, const float4* acc, float dt, int n, cudaStream_t s);
 void launch_drift(BodyArrays b, double dt, int n, cudaStream_t s);
+// Ensemble step opening (kick by hdt, then drift by dt; the same arithmetic as the two kernels).
+void launch_kick_drift(BodyArrays b, const float4* acc, float hdt, double dt, int n, cudaStream_t s);
+// out[2 s], out[2 s + 1] = kinetic and potential energy of system s (bodies [off[s], off[s + 1])).
+void launch_sys_energy(const BodyArrays b, const float4* acc, const uint32_t* off, int nsys, double* out,
+                       cudaStream_t s);
 // Diagnostics: out[13] = mass, ke, sum m phi, px, py, pz, lx, ly, lz, mx, my, mz, (unused).
 void launch_diag(const BodyArrays b, const float4* acc, int n, double* partial, unsigned* ticket, double* out,
                  int blocks, cudaStream_t s);
@@ -59,5 +64,16 @@ void launch_flush(float* buf, size_t count, cudaStream_t s);
 void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential, bool eps0, const DirectShape& shape,
                    float4* acc, float4* partial, unsigned* err, cudaStream_t s);
 DirectShape default_direct_shape(int n, int sms);
+// Batched direct sums over independent systems: one block per work item, i-bodies [base, iend)
+// (at most direct_block_bodies(ipt) of them) against j-bodies [j0, j1) of the same system, with
+// that system's squared softening e2. Writes G-scaled accelerations and potentials.
+struct alignas(32) DirectWork {
+    int base, iend, j0, j1;
+    float e2;
+    int sys, pad0, pad1;
+};
+int direct_block_bodies(int ipt);
+void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, float G, bool potential,
+                         bool eps0, float4* acc, unsigned* err, cudaStream_t s);
 
 }  // namespace lg

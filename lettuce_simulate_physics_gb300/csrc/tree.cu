@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -92,6 +93,17 @@ struct TreeState {
     bool restart_mode = false;  // key restarts were needed last time: check for them on the host
     bool speculative = false;   // the current build used guessed sizes / assumed no restart
     double theta = 0.6;
+    // Forest (ensemble) configuration: the tree covers bodies [0, n_tree) of nsys systems whose
+    // ranges are sys_off[0..nsys] (device); sys[i] is body i's system (device); per-system inverse
+    // opening angles. n_tree < 0 means one system over all bodies.
+    int n_tree = -1;
+    int nsys = 1;
+    const uint32_t* sys = nullptr;
+    const uint32_t* sys_off = nullptr;
+    const float* inv_theta_sys = nullptr;
+    uint64_t generation = 0;  // bumped by every build that may grow (reallocate) tree buffers
+    DevBuf mkeys;   // forest: Morton keys before the (system, key) sort
+    DevBuf sticky;  // graph mode: sticky word set when a sync-free build misses
 };
 
 namespace {
@@ -126,12 +138,19 @@ __device__ __forceinline__ uint64_t morton(double x, double y, double z, double 
 // Common octal prefix (0..21) of two 63-bit keys.
 __device__ __forceinline__ int cpl21(uint64_t a, uint64_t b) { return (__clzll(a ^ b) - 1) / 3; }
 
-// Common octal prefix (0..42) of composite keys (key, restart key).
-__device__ __forceinline__ int cpl42(const uint64_t* k0, const uint64_t* k1, int i, int j) {
+// Forest builds (many independent systems in one pipeline) pass a per-body system index `sys`:
+// bodies of different systems share no prefix (-1), so no leaf, node or group spans two systems.
+// Single-system builds pass null.
+
+// Common octal prefix (0..42) of composite keys (key, restart key); -1 across systems.
+__device__ __forceinline__ int cpl42(const uint32_t* sys, const uint64_t* k0, const uint64_t* k1, int i, int j) {
+    if (sys && sys[i] != sys[j]) return -1;
     const uint64_t a = k0[i], b = k0[j];
     if (a != b || !k1) return cpl21(a, b);
     return MAX_LEVEL + cpl21(k1[i], k1[j]);
 }
+
+__device__ __forceinline__ uint32_t sys_of(const uint32_t* sys, int i) { return sys ? sys[i] : 0u; }
 
 // Octal digit of composite key at depth d (1-based).
 __device__ __forceinline__ int digit_at(const uint64_t* k0, const uint64_t* k1, int i, int d) {
@@ -211,12 +230,60 @@ __global__ void k_frame(const BodyArrays b, int n, double* partial, unsigned* ti
     }
 }
 
-__global__ void k_keys(const BodyArrays b, int n, const double* __restrict__ frame, uint64_t* __restrict__ keys,
-                       uint32_t* __restrict__ vals) {
+__global__ void k_keys(const uint32_t* __restrict__ sys, const BodyArrays b, int n, const double* __restrict__ frame,
+                       uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    keys[i] = morton(b.x[i], b.y[i], b.z[i], frame[0], frame[1], frame[2], frame[4]);
+    const double* f = frame + 5 * sys_of(sys, i);
+    keys[i] = morton(b.x[i], b.y[i], b.z[i], f[0], f[1], f[2], f[4]);
     vals[i] = static_cast<uint32_t>(i);
+}
+
+// Forest: one block per system computes its key frame over its body range [off[s], off[s + 1]).
+__global__ void k_frame_sys(const BodyArrays b, const uint32_t* __restrict__ off, double* frame) {
+    __shared__ double sh[6][BS / 32];
+    const uint32_t lo = off[blockIdx.x], hi = off[blockIdx.x + 1];
+    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += BS) {
+        const double p[3] = {b.x[i], b.y[i], b.z[i]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = fmin(v[c], p[c]);
+            v[3 + c] = fmax(v[3 + c], p[c]);
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
+        }
+        if (lane == 0) sh[c][w] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r[6];
+        for (int c = 0; c < 6; ++c) {
+            r[c] = sh[c][0];
+            for (int u = 1; u < BS / 32; ++u) r[c] = c < 3 ? fmin(r[c], sh[c][u]) : fmax(r[c], sh[c][u]);
+        }
+        double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
+        side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
+        double* f = frame + 5 * blockIdx.x;
+        f[0] = r[0];
+        f[1] = r[1];
+        f[2] = r[2];
+        f[3] = side;
+        f[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
+    }
+}
+
+// keys[i] = (system of body vals[i]): the second key of the forest's (system, Morton) sort.
+__global__ void k_sys_keys(const uint32_t* __restrict__ sys, const uint32_t* __restrict__ vals,
+                           uint64_t* __restrict__ keys, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = sys_of(sys, static_cast<int>(vals[i]));
 }
 
 // ---- onesweep radix sort ---------------------------------------------------------------------
@@ -401,11 +468,20 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
 // copies the sorted keys; optionally carries a second key array through the permutation.
 __global__ void k_permute(const BodyArrays src, BodyArrays dst, const uint64_t* __restrict__ keys,
                           const uint32_t* __restrict__ vals, uint64_t* __restrict__ skey,
-                          const uint64_t* __restrict__ key1_in, uint64_t* __restrict__ key1_out, int n) {
+                          const uint64_t* __restrict__ key1_in, uint64_t* __restrict__ key1_out, int n,
+                          const uint64_t* __restrict__ key_src, int n_total) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t j = vals[i];
-    skey[i] = keys[i];
+    if (i >= n_total) return;
+    // Bodies past the tree's range (the forest's direct systems) keep their place.
+    const uint32_t j = i < n ? vals[i] : static_cast<uint32_t>(i);
+    if (i < n) skey[i] = key_src ? key_src[j] : keys[i];
+    if (i >= n) {
+        dst.x[i] = src.x[i]; dst.y[i] = src.y[i]; dst.z[i] = src.z[i];
+        dst.hm[i] = src.hm[i]; dst.lo[i] = src.lo[i];
+        dst.vx[i] = src.vx[i]; dst.vy[i] = src.vy[i]; dst.vz[i] = src.vz[i];
+        dst.m[i] = src.m[i]; dst.id[i] = src.id[i]; dst.cost[i] = src.cost[i];
+        return;
+    }
     if (key1_in) key1_out[i] = key1_in[j];
     dst.x[i] = src.x[j];
     dst.y[i] = src.y[j];
@@ -501,16 +577,18 @@ __global__ void __launch_bounds__(SCAN_BS) k_scan(const uint32_t* __restrict__ i
 
 // ---- key restarts ----------------------------------------------------------------------------
 // A run of identical frame-0 keys longer than LEAF_MAX: appended as (start, end).
-__global__ void k_find_runs(const uint64_t* __restrict__ skey, int n, uint2* runs, unsigned* count, int cap) {
+__global__ void k_find_runs(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ skey, int n, uint2* runs,
+                            unsigned* count, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i + LEAF_MAX >= n) return;
     const uint64_t k = skey[i];
-    if (i > 0 && skey[i - 1] == k) return;
-    if (skey[i + LEAF_MAX] != k) return;
-    int lo = i + LEAF_MAX, hi = n;  // first index with a different key
+    const uint32_t sy = sys_of(sys, i);
+    if (i > 0 && skey[i - 1] == k && sys_of(sys, i - 1) == sy) return;
+    if (skey[i + LEAF_MAX] != k || sys_of(sys, i + LEAF_MAX) != sy) return;
+    int lo = i + LEAF_MAX, hi = n;  // first index with a different (system, key)
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (skey[mid] == k) lo = mid + 1;
+        if (skey[mid] == k && sys_of(sys, mid) == sy) lo = mid + 1;
         else hi = mid;
     }
     const unsigned r = atomicAdd(count, 1u);
@@ -601,7 +679,8 @@ __global__ void k_gather_keys(const uint64_t* __restrict__ src, const uint32_t* 
 constexpr int DEPTH_BS = 256;
 constexpr int GMAX_LIMIT = 1024;
 
-__global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+__global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0,
+                                                         const uint64_t* __restrict__ k1,
                                                          const int* __restrict__ runid, const double* __restrict__ cube,
                                                          int n, int gmax, uint16_t* __restrict__ bdepth) {
     __shared__ int8_t c16[DEPTH_BS + LEAF_MAX];
@@ -610,11 +689,11 @@ __global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint64_t* __restr
     // Window starts j in [i0 - w, i0 + DEPTH_BS): slot j - (i0 - w).
     for (int t = threadIdx.x; t < DEPTH_BS + LEAF_MAX; t += DEPTH_BS) {
         const int j = i0 - LEAF_MAX + t;
-        c16[t] = static_cast<int8_t>((j >= 0 && j + LEAF_MAX < n) ? cpl42(k0, k1, j, j + LEAF_MAX) : -1);
+        c16[t] = static_cast<int8_t>((j >= 0 && j + LEAF_MAX < n) ? cpl42(sys, k0, k1, j, j + LEAF_MAX) : -1);
     }
     for (int t = threadIdx.x; t < DEPTH_BS + gmax; t += DEPTH_BS) {
         const int j = i0 - gmax + t;
-        cg[t] = static_cast<int8_t>((j >= 0 && j + gmax < n) ? cpl42(k0, k1, j, j + gmax) : -1);
+        cg[t] = static_cast<int8_t>((j >= 0 && j + gmax < n) ? cpl42(sys, k0, k1, j, j + gmax) : -1);
     }
     __syncthreads();
     const int i = i0 + threadIdx.x;
@@ -632,18 +711,18 @@ __global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint64_t* __restr
     bdepth[i] = static_cast<uint16_t>(ld | (gd << 8));
 }
 
-__global__ void k_leaf_flags(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+__global__ void k_leaf_flags(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
                              const uint16_t* __restrict__ bdepth, int n, uint32_t* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int d = bdepth[i] & 255;
     uint32_t f = 1;
-    if (i > 0 && (bdepth[i - 1] & 255) == d && cpl42(k0, k1, i - 1, i) >= d) f = 0;
+    if (i > 0 && (bdepth[i - 1] & 255) == d && cpl42(sys, k0, k1, i - 1, i) >= d) f = 0;
     flag[i] = f;
 }
 
 // leaf_first, leaf_depth, leaf_c, and the node count of each leaf (its owned ancestors + itself).
-__global__ void k_leaf_info(const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+__global__ void k_leaf_info(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
                             const uint16_t* __restrict__ bdepth, const uint32_t* __restrict__ flag,
                             const uint32_t* __restrict__ lid, int n, uint32_t* leaf_first, uint8_t* leaf_depth,
                             int8_t* leaf_c, uint32_t* leaf_nodes, int* max_depth) {
@@ -652,7 +731,7 @@ __global__ void k_leaf_info(const uint64_t* __restrict__ k0, const uint64_t* __r
     const uint32_t l = lid[i];
     const int d = bdepth[i] & 255;
     atomicMax(max_depth, d);
-    const int c = i == 0 ? -1 : cpl42(k0, k1, i - 1, i);
+    const int c = i == 0 ? -1 : cpl42(sys, k0, k1, i - 1, i);
     leaf_first[l] = static_cast<uint32_t>(i);
     leaf_depth[l] = static_cast<uint8_t>(d);
     leaf_c[l] = static_cast<int8_t>(c);
@@ -661,6 +740,7 @@ __global__ void k_leaf_info(const uint64_t* __restrict__ k0, const uint64_t* __r
 
 // ---- nodes -----------------------------------------------------------------------------------
 struct NodeCtx {
+    const uint32_t* sys;  // per-body system (forest) or null
     const uint64_t* k0;
     const uint64_t* k1;
     const uint32_t* leaf_first;  // K+1
@@ -672,6 +752,7 @@ struct NodeCtx {
     int n;
     const unsigned* Kdev;  // leaf count (device)
     unsigned Kcap;         // capacity the leaf arrays were sized for
+    unsigned nroots;       // systems in the forest (1 for one system); roots take node indices 0..nroots-1
 };
 
 __device__ __forceinline__ int leaf_count(const NodeCtx& c) { return static_cast<int>(min(*c.Kdev, c.Kcap)); }
@@ -688,7 +769,7 @@ __device__ __forceinline__ uint32_t range_end(const NodeCtx& c, uint32_t lo, int
     uint32_t a = lo + 1, b = static_cast<uint32_t>(c.n);
     while (a < b) {
         uint32_t mid = (a + b) >> 1;
-        if (cpl42(c.k0, c.k1, lo, mid) >= d) a = mid + 1;
+        if (cpl42(c.sys, c.k0, c.k1, lo, mid) >= d) a = mid + 1;
         else b = mid;
     }
     return a;
@@ -751,10 +832,10 @@ __global__ void k_cpu_index(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, cons
                             const uint16_t* pn_meta, const uint32_t* pn_cb, uint32_t* pn_cpu) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= eff(Tdev, Tcap)) return;
-    if (v == 0) pn_cpu[0] = 0;
     const uint16_t meta = pn_meta[v];
+    if ((meta & 255) == 0) pn_cpu[v] = sys_of(c.sys, static_cast<int>(pn_lohi[v].x));  // a system's root
     if (meta & 256) return;
-    const uint32_t first = 1 + pn_cb[v];
+    const uint32_t first = c.nroots + pn_cb[v];
     for_children(c, pn_lohi, v, meta & 255, [&](int k, uint32_t ch) { pn_cpu[ch] = first + k; });
 }
 
@@ -762,6 +843,7 @@ __global__ void k_cpu_index(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, cons
 // 585-592) of the node at depth d containing body b; restart cube at depth 21 for restarted runs.
 __device__ void node_geo(const NodeCtx& c, const double* frame, const int* runid, const double* cube, uint32_t b,
                          int d, double& gx, double& gy, double& gz, double& half) {
+    frame += 5 * sys_of(c.sys, static_cast<int>(b));
     half = 0.5 * frame[3];
     gx = __dadd_rn(frame[0], half);
     gy = __dadd_rn(frame[1], half);
@@ -799,7 +881,7 @@ __global__ void k_nodes_out(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, cons
     const uint2 r = pn_lohi[v];
     const uint32_t me = pn_cpu[v];
     const uint32_t nch = pn_nchild[v];
-    const uint32_t first = leaf ? r.x : 1 + pn_cb[v];
+    const uint32_t first = leaf ? r.x : c.nroots + pn_cb[v];
     if (me >= T || (!leaf && first + nch > T) || r.x >= r.y || r.y > static_cast<uint32_t>(c.n)) {
         atomicOr(err, kErrNodeOverflow);
         return;
@@ -948,7 +1030,7 @@ __global__ void k_upsweep_offsets(UpsweepIndex* ix) {
 __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t Kcap, const unsigned* Kdev,
                                uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
                                const float4* __restrict__ nd_geo, const BodyArrays b, Moments mo, float inv_theta,
-                               unsigned* err) {
+                               const float* __restrict__ inv_theta_sys, const uint32_t* __restrict__ sys, unsigned* err) {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t T = eff(Tdev, Tcap);
     if (l >= eff(Kdev, Kcap)) return;
@@ -959,6 +1041,7 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
     }
     const uint4 r = nd_range[node];
     const float4 g = nd_geo[node];
+    if (inv_theta_sys) inv_theta = inv_theta_sys[sys_of(sys, static_cast<int>(r.x))];
     double M = 0, sx = 0, sy = 0, sz = 0;
     for (uint32_t i = r.x; i < r.y; ++i) {
         const double m = b.m[i];
@@ -993,7 +1076,9 @@ __device__ __forceinline__ double shfl8(double v, int src_lane) { return __shfl_
 
 __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth,
                                 uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
-                                const float4* __restrict__ nd_geo, Moments mo, float inv_theta, unsigned* err) {
+                                const float4* __restrict__ nd_geo, Moments mo, float inv_theta,
+                                const float* __restrict__ inv_theta_sys, const uint32_t* __restrict__ sys,
+                                unsigned* err) {
     const uint32_t T = eff(Tdev, Tcap);
     const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
     const int lane = threadIdx.x & 31, sub = lane >> 3, j = lane & 7, base_lane = lane & ~7;
@@ -1066,7 +1151,9 @@ __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const Up
                 qyz = DADD(qyz, vyz);
             }
         }
-        if (valid && j == 0) store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
+        if (valid && j == 0)
+            store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g,
+                          inv_theta_sys ? inv_theta_sys[sys_of(sys, static_cast<int>(r.x))] : inv_theta);
     }
 }
 
@@ -1148,26 +1235,43 @@ const void* probe_kernel() { return reinterpret_cast<const void*>(k_probe); }
 
 void tree_sort(Engine& e) {
     TreeState& t = *e.tree;
-    const int n = e.n;
+    const int n = t.n_tree >= 0 ? t.n_tree : e.n;
+    const int n_total = e.n;
+    const uint32_t* sys = t.sys;
     cudaStream_t s = e.stream;
     if (n >= (1 << 30)) fail(kRuntime, "cuda tree: n >= 2^30 exceeds the sort's look-back counters");
     reserve_sort(t, n);
-    t.frame.reserve(64);
+    t.frame.reserve(static_cast<size_t>(std::max(t.nsys, 1)) * 5 * 8 + 64);
     t.counts.reserve(64);
     t.restarted = false;
     t.nruns = 0;
-    const int fb = std::min(2 * e.sms, grid_for(n, BS));
-    e.diag_partial.reserve(static_cast<size_t>(fb) * 12 * 8);
-    k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<double>(), e.ticket(), t.frame.as<double>());
+    if (sys) {
+        k_frame_sys<<<t.nsys, BS, 0, s>>>(e.bodies(e.cur), t.sys_off, t.frame.as<double>());
+    } else {
+        const int fb = std::min(2 * e.sms, grid_for(n, BS));
+        e.diag_partial.reserve(static_cast<size_t>(fb) * 12 * 8);
+        k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<double>(), e.ticket(), t.frame.as<double>());
+    }
     LG_LAUNCHED();
-    k_keys<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), n, t.frame.as<double>(), t.keysA.as<uint64_t>(),
-                                          t.valsA.as<uint32_t>());
+    if (sys) t.mkeys.reserve(static_cast<size_t>(n) * 8 + 8);
+    k_keys<<<grid_for(n, BS), BS, 0, s>>>(sys, e.bodies(e.cur), n, t.frame.as<double>(),
+                                          sys ? t.mkeys.as<uint64_t>() : t.keysA.as<uint64_t>(), t.valsA.as<uint32_t>());
     LG_LAUNCHED();
     e.launches += 2;
+    if (sys) LG_CK(cudaMemcpyAsync(t.keysA.as<uint64_t>(), t.mkeys.as<uint64_t>(), static_cast<size_t>(n) * 8,
+                                   cudaMemcpyDeviceToDevice, s));
     sort_pairs(e, t, n);
+    if (sys) {
+        // Forest: stable sort by system on top of the key order -> (system, key) order.
+        k_sys_keys<<<grid_for(n, BS), BS, 0, s>>>(sys, t.valsA.as<uint32_t>(), t.keysA.as<uint64_t>(), n);
+        LG_LAUNCHED();
+        ++e.launches;
+        sort_pairs(e, t, n);
+    }
     int other = e.cur ^ 1;
-    k_permute<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
-                                             t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), nullptr, nullptr, n);
+    k_permute<<<grid_for(n_total, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
+                                                   t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), nullptr, nullptr, n,
+                                                   sys ? t.mkeys.as<uint64_t>() : nullptr, n_total);
     LG_LAUNCHED();
     ++e.launches;
     e.cur = other;
@@ -1177,7 +1281,7 @@ void tree_sort(Engine& e) {
     LG_CK(cudaMemsetAsync(counts, 0, 64, s));
     const int run_cap = std::max(1, n / (LEAF_MAX + 1) + 1);
     t.runs.reserve(static_cast<size_t>(run_cap) * 8);
-    k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), n, t.runs.as<uint2>(), counts, run_cap);
+    k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(sys, t.skey.as<uint64_t>(), n, t.runs.as<uint2>(), counts, run_cap);
     LG_LAUNCHED();
     ++e.launches;
     // Key restarts are rare: unless the last build needed them, assume none and let the check after
@@ -1191,6 +1295,7 @@ void tree_sort(Engine& e) {
     if (R == 0) return;
     t.nruns = R;
     t.restarted = true;
+    ++t.generation;
     BodyArrays b = e.bodies(e.cur);
     t.runcube.reserve(static_cast<size_t>(R) * 5 * 8);
     t.runid.reserve(static_cast<size_t>(n) * 4);
@@ -1216,10 +1321,21 @@ void tree_sort(Engine& e) {
     LG_LAUNCHED();
     e.launches += 2;
     sort_pairs(e, t, n);
+    if (sys) {
+        // Equal keys of different systems must not interleave: systems on top.
+        k_sys_keys<<<grid_for(n, BS), BS, 0, s>>>(sys, t.valsA.as<uint32_t>(), t.keysA.as<uint64_t>(), n);
+        LG_LAUNCHED();
+        ++e.launches;
+        sort_pairs(e, t, n);
+        k_gather_keys<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), t.valsA.as<uint32_t>(),
+                                                     t.keysA.as<uint64_t>(), n);
+        LG_LAUNCHED();
+        ++e.launches;
+    }
     other = e.cur ^ 1;
-    k_permute<<<grid_for(n, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
-                                             t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), key1,
-                                             t.skey1.as<uint64_t>(), n);
+    k_permute<<<grid_for(n_total, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
+                                                   t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), key1,
+                                                   t.skey1.as<uint64_t>(), n, nullptr, n_total);
     LG_LAUNCHED();
     ++e.launches;
     e.cur = other;
@@ -1227,7 +1343,8 @@ void tree_sort(Engine& e) {
 
 void tree_build(Engine& e, double theta) {
     TreeState& t = *e.tree;
-    const int n = e.n;
+    const int n = t.n_tree >= 0 ? t.n_tree : e.n;
+    const uint32_t* sys = t.sys;
     cudaStream_t s = e.stream;
     t.group_max = e.group_max;
     t.theta = theta;
@@ -1250,14 +1367,15 @@ void tree_build(Engine& e, double theta) {
     t.leaf_node.reserve(n1 * 4);
     const int gb = grid_for(n, BS);
     if (t.group_max > GMAX_LIMIT) fail(kRuntime, "cuda tree build: group size above 1024");
-    k_body_depth<<<grid_for(n, DEPTH_BS), DEPTH_BS, 0, s>>>(k0, k1, runid, cube, n, t.group_max, t.bdepth.as<uint16_t>());
+    k_body_depth<<<grid_for(n, DEPTH_BS), DEPTH_BS, 0, s>>>(sys, k0, k1, runid, cube, n, t.group_max,
+                                                            t.bdepth.as<uint16_t>());
     LG_LAUNCHED();
-    k_leaf_flags<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
+    k_leaf_flags<<<gb, BS, 0, s>>>(sys, k0, k1, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
     LG_LAUNCHED();
     e.launches += 2;
     scan_u32(e, t, t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n, counts + 1);
     LG_CK(cudaMemsetAsync(t.leaf_cnt.as<char>(), 0, n1 * 4, s));
-    k_leaf_info<<<gb, BS, 0, s>>>(k0, k1, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
+    k_leaf_info<<<gb, BS, 0, s>>>(sys, k0, k1, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
                                   t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
                                   t.leaf_cnt.as<uint32_t>(), reinterpret_cast<int*>(counts + 4));
     LG_LAUNCHED();
@@ -1284,13 +1402,19 @@ void tree_build(Engine& e, double theta) {
         const int dx = static_cast<int>(e.pinned_small[4]);
         if (Kx < 1 || Kx > static_cast<size_t>(n) || Tx < Kx)
             fail(kRuntime, "cuda tree build: bad leaf/node count " + std::to_string(Kx) + "/" + std::to_string(Tx));
-        K = std::min(static_cast<size_t>(n), Kx + Kx / 4 + 1024);
-        T = Tx + Tx / 4 + 1024;
-        depth = std::min(dx + 2, MAX_DEPTH + 1);
+        // Headroom for the sync-free builds that follow (LETTUCE_GB300_TREE_HEADROOM percent, default
+        // 25, plus a fixed slack unless it is 0): more memory against fewer exact rebuilds.
+        size_t pct = 25;
+        if (const char* h = std::getenv("LETTUCE_GB300_TREE_HEADROOM")) pct = static_cast<size_t>(std::atoi(h));
+        const size_t slack = pct ? 1024 : 0;
+        K = std::min(static_cast<size_t>(n), Kx + Kx * pct / 100 + slack);
+        T = Tx + Tx * pct / 100 + slack;
+        depth = std::min(dx + (pct ? 2 : 0), MAX_DEPTH + 1);
         t.K = K;
         t.T = T;
         t.max_depth = depth;
         t.have_guess = true;
+        ++t.generation;
         t.speculative = false;
     }
     t.pn_lohi.reserve(T * 8);
@@ -1306,8 +1430,9 @@ void tree_build(Engine& e, double theta) {
     for (DevBuf* d : {&t.nd_range, &t.nd_com, &t.nd_comlo, &t.nd_q0, &t.nd_q1, &t.nd_geo}) d->reserve(T * 16);
     t.nd_parent.reserve(T * 4);
     const uint32_t Tc = static_cast<uint32_t>(T), Kc = static_cast<uint32_t>(K);
-    NodeCtx c{k0, k1, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
-              t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, Kdev, Kc};
+    NodeCtx c{sys, k0, k1, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
+              t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, Kdev, Kc,
+              static_cast<unsigned>(sys ? t.nsys : 1)};
     const int tb = grid_for(static_cast<long long>(T), BS);
     // Index arrays start out of range (0xff..): a slot the construction fails to fill is caught by
     // the range checks below instead of being followed.
@@ -1358,13 +1483,13 @@ void tree_build(Engine& e, double theta) {
     Moments mo{t.nd_com.as<float4>(), t.nd_comlo.as<float4>(), t.nd_q0.as<float4>(), t.nd_q1.as<float4>()};
     k_leaf_moments<<<grid_for(static_cast<long long>(K), 128), 128, 0, s>>>(
         t.leaf_order.as<uint32_t>(), Kc, Kdev, Tc, Tdev, t.nd_range.as<uint4>(), t.nd_geo.as<float4>(), e.bodies(e.cur),
-        mo, inv_theta, e.err_word());
+        mo, inv_theta, t.inv_theta_sys, sys, e.err_word());
     LG_LAUNCHED();
     e.launches += 4;
     const int cb = std::max(1, std::min(4 * e.sms, grid_for(static_cast<long long>(T), 128)));
     for (int d = depth - 1; d >= 0; --d) {
         k_combine_level<<<cb, 128, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, Tc, Tdev, t.nd_range.as<uint4>(),
-                                           t.nd_geo.as<float4>(), mo, inv_theta, e.err_word());
+                                           t.nd_geo.as<float4>(), mo, inv_theta, t.inv_theta_sys, sys, e.err_word());
         LG_LAUNCHED();
         ++e.launches;
     }
@@ -1387,6 +1512,41 @@ bool tree_verify(Engine& e, const unsigned* counts_host) {
 }
 
 const unsigned* tree_counts_device(Engine& e) { return e.tree->counts.as<unsigned>(); }
+
+namespace {
+// Sets *sticky when the build just launched exceeded what it was launched for, or a key restart
+// was needed: the same test as tree_verify, on the device, for step loops without host reads.
+__global__ void k_tree_check(const unsigned* __restrict__ counts, unsigned K, unsigned T, int depth, int restarted,
+                             unsigned* sticky) {
+    const bool ok = (restarted || counts[0] == 0) && counts[1] <= K && counts[2] <= T &&
+                    static_cast<int>(counts[4]) <= depth;
+    if (!ok) atomicOr(sticky, 1u);
+}
+}  // namespace
+
+void tree_set_forest(Engine& e, int n_tree, int nsys, const uint32_t* sys, const uint32_t* sys_off,
+                     const float* inv_theta_sys) {
+    TreeState& t = *e.tree;
+    t.n_tree = n_tree;
+    t.nsys = nsys;
+    t.sys = sys;
+    t.sys_off = sys_off;
+    t.inv_theta_sys = inv_theta_sys;
+    t.have_guess = false;
+    t.restart_mode = false;
+}
+
+bool tree_sync_free_ready(const Engine& e) { return e.tree->have_guess && !e.tree->restart_mode; }
+uint64_t tree_generation(const Engine& e) { return e.tree->generation; }
+
+void tree_check_async(Engine& e, unsigned* sticky) {
+    TreeState& t = *e.tree;
+    if (!t.speculative) return;
+    k_tree_check<<<1, 1, 0, e.stream>>>(t.counts.as<unsigned>(), static_cast<unsigned>(t.K),
+                                        static_cast<unsigned>(t.T), t.max_depth, t.restarted ? 1 : 0, sticky);
+    LG_LAUNCHED();
+    ++e.launches;
+}
 void tree_reset_guess(Engine& e) {
     e.tree->have_guess = false;
     e.tree->restart_mode = false;

@@ -61,6 +61,10 @@ struct WalkArgs {
     unsigned long long* inter;
     unsigned* err;
     float G, e2;
+    // Forest (ensemble) walk: body -> system (nullptr: one tree rooted at node 0) and the
+    // per-system squared softening; system s's tree is rooted at node s.
+    const uint32_t* sys;
+    const float* e2_sys;
 };
 
 __device__ __forceinline__ int warp_excl_scan(int v, int lane, int& total) {
@@ -209,7 +213,7 @@ constexpr float kFar = 1e18f;
 template <bool POT, bool EPS0>
 __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int ipt, int nc, int nr, float ox,
                                       float oy, float oz, const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
-                                      const float (&zi)[IPT_MAX]) {
+                                      const float (&zi)[IPT_MAX], float e2) {
     for (int c0 = 0; c0 < nc; c0 += CCH) {
         const int cc = min(CCH, nc - c0);
         const int cc2 = (cc + 1) & ~1;
@@ -228,7 +232,7 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
             }
         }
         __syncwarp();
-        eval_cells_n<POT, EPS0>(ipt, s, cc2, lane, xi, yi, zi, w.e2);
+        eval_cells_n<POT, EPS0>(ipt, s, cc2, lane, xi, yi, zi, e2);
         __syncwarp();
     }
     if (nr == 0) return;
@@ -268,7 +272,7 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
             }
         }
         __syncwarp();
-        eval_bodies_n<POT, EPS0>(ipt, s, bc2, lane, xi, yi, zi, w.e2);
+        eval_bodies_n<POT, EPS0>(ipt, s, bc2, lane, xi, yi, zi, e2);
         __syncwarp();
     }
 }
@@ -293,8 +297,10 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
 #pragma unroll
         for (int f = 0; f < 8; ++f) s.ks[u][f][lane] = 0.f;
     const unsigned lt = (1u << lane) - 1u;
+    const uint32_t root = w.sys ? w.sys[gr.x] : 0u;
+    const float e2 = w.e2_sys ? w.e2_sys[root] : w.e2;
     int sp = 1;
-    if (lane == 0) stack[0] = 0;
+    if (lane == 0) stack[0] = root;
     __syncwarp();
     int nc = 0, nr = 0, nbr = 0;
     uint32_t list_len = 0, cells_len = 0;
@@ -306,7 +312,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         const bool done = sp == 0;
         // One evaluation site: when the lists fill up, and once at the end.
         if (done || nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
-            flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi);
+            flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2);
             list_len += nc + nbr;
             cells_len += nc;
             nc = nr = nbr = 0;
@@ -366,7 +372,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         __syncwarp();
     }
     if (overflow && lane == 0) atomicOr(w.err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
-    const float self_inv = (POT && !EPS0) ? rsqrt_mufu(w.e2) : 0.f;
+    const float self_inv = (POT && !EPS0) ? rsqrt_mufu(e2) : 0.f;
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
         const int k = lane + 32 * u;
@@ -426,8 +432,10 @@ int walk_blocks(int sms) {
 
 }  // namespace
 
-void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0) {
+void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys, const float* e2_sys) {
     WalkArgs w;
+    w.sys = sys;
+    w.e2_sys = e2_sys;
     w.tv = tree_view(e);
     BodyArrays b = e.bodies(e.cur);
     w.hm = b.hm;

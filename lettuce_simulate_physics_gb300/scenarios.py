@@ -11,6 +11,7 @@ Workloads (sizes are the defaults):
   disk(n=1_000_000, seed=1)              exponential disk, sech^2 vertical, core mass 1
   collision(n_each=8_000_000)            two inclined disks on a parabolic orbit
   ensemble_sizes(512)                    log-uniform cluster sizes in [1024, 131072]
+  ensemble(512)                          512 Plummer clusters back to back (seeds 100-611)
 Test shapes mirroring the reference tests: plummer(n, seed, cut=20), cube(n, seed).
 """
 from __future__ import annotations
@@ -199,3 +200,24 @@ def ensemble_sizes(count: int = 512, lo: int = 1024, hi: int = 131072, seed: int
 def ensemble_eps(n: np.ndarray, base: float = 0.01, n0: int = 16384) -> np.ndarray:
     """Per-system softening eps = base * (N / n0)^(-1/3)."""
     return base * (np.asarray(n, np.float64) / n0) ** (-1.0 / 3.0)
+
+
+def ensemble(count: int = 512, lo: int = 1024, hi: int = 131072, seed0: int = 100, direct_max: int = 8192,
+             theta: float = 0.5, sizes=None):
+    """Independent Plummer clusters (plummer() recipe, seeds seed0 + s, each centred) back to back.
+
+    Sizes are ensemble_sizes(count, lo, hi, seed0) unless given; softening ensemble_eps(N); direct
+    summation for N <= direct_max, tree with opening angle ``theta`` above. Ids run 0..total-1.
+    Returns (Bodies, counts, eps, thetas, methods) with methods 0 = direct, 1 = tree.
+    """
+    n = np.asarray(ensemble_sizes(count, lo, hi, seed0) if sizes is None else sizes, np.int64)
+    pos, vel, m = [], [], []
+    for s, ns in enumerate(n):
+        p, v, ms = plummer_arrays(int(ns), seed0 + s)
+        M = ms.sum()
+        pos.append(p - (ms[:, None] * p).sum(0) / M)
+        vel.append(v - (ms[:, None] * v).sum(0) / M)
+        m.append(ms)
+    b = Bodies.from_arrays(np.concatenate(pos), np.concatenate(vel), np.concatenate(m))
+    methods = np.where(n <= direct_max, 0, 1).astype(np.int32)
+    return b, n.astype(np.uint32), ensemble_eps(n), np.full(len(n), float(theta)), methods
