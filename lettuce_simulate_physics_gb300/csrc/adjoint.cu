@@ -23,6 +23,13 @@
 // Checkpoints: FP64 positions and FP32 velocities every k steps; the backward pass restores each
 // segment, recomputes its positions with the same deterministic kernels (so they are bit-identical
 // to the forward pass), and stores them as hi/lo float4 pairs for the VJP.
+//
+// Tree forces (Barnes-Hut with quadrupoles): the same sweep with the tree walk's VJP (walk_vjp.cu)
+// over frozen interaction lists. The tree sorts the bodies every step, so the adjoint state is
+// indexed by body id (ids 0..n-1), checkpoints also keep masses and ids, and the segment store
+// keeps each step's FP64 positions in the order its force call sorted them. For the VJP of step s
+// the backward pass loads those positions and rebuilds the tree: the sort of already sorted bodies
+// is the identity, so the tree, its moments and its lists are bit-identical to the forward pass's.
 #include <algorithm>
 #include <vector>
 
@@ -188,24 +195,88 @@ __global__ void k_adj_init(const BodyArrays b, const double* tx, const double* t
     loss_terms[i] = m * d2;
 }
 
-// Checkpoint copy of the state: FP64 positions, FP32 velocities.
-__global__ void k_save(const BodyArrays b, double* x, double* y, double* z, float* vx, float* vy, float* vz, int n) {
+// Checkpoint copy of the state: FP64 positions, FP32 velocities, masses and ids (the tree
+// reorders the bodies).
+__global__ void k_save(const BodyArrays b, double* x, double* y, double* z, float* vx, float* vy, float* vz, float* m,
+                       uint32_t* id, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     x[i] = b.x[i]; y[i] = b.y[i]; z[i] = b.z[i];
     vx[i] = b.vx[i]; vy[i] = b.vy[i]; vz[i] = b.vz[i];
+    m[i] = b.m[i]; id[i] = b.id[i];
+}
+
+__device__ __forceinline__ void set_pos(BodyArrays b, int i, double px, double py, double pz, float m) {
+    b.x[i] = px; b.y[i] = py; b.z[i] = pz;
+    const float hx = __double2float_rn(px), hy = __double2float_rn(py), hz = __double2float_rn(pz);
+    b.hm[i] = make_float4(hx, hy, hz, m);
+    b.lo[i] = make_float4(__double2float_rn(px - hx), __double2float_rn(py - hy), __double2float_rn(pz - hz), 0.f);
 }
 
 __global__ void k_restore(BodyArrays b, const double* x, const double* y, const double* z, const float* vx,
-                          const float* vy, const float* vz, int n) {
+                          const float* vy, const float* vz, const float* m, const uint32_t* id, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double px = x[i], py = y[i], pz = z[i];
-    b.x[i] = px; b.y[i] = py; b.z[i] = pz;
     b.vx[i] = vx[i]; b.vy[i] = vy[i]; b.vz[i] = vz[i];
-    const float hx = __double2float_rn(px), hy = __double2float_rn(py), hz = __double2float_rn(pz);
-    b.hm[i] = make_float4(hx, hy, hz, b.m[i]);
-    b.lo[i] = make_float4(__double2float_rn(px - hx), __double2float_rn(py - hy), __double2float_rn(pz - hz), 0.f);
+    b.m[i] = m[i]; b.id[i] = id[i];
+    set_pos(b, i, x[i], y[i], z[i], m[i]);
+}
+
+// Tree path: one step's positions (in its sorted order) and ids, and back.
+__global__ void k_store_step(const BodyArrays b, double* x, double* y, double* z, uint32_t* id, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = b.x[i]; y[i] = b.y[i]; z[i] = b.z[i]; id[i] = b.id[i];
+}
+
+__global__ void k_load_step(BodyArrays b, const double* x, const double* y, const double* z, const uint32_t* id,
+                            const float* m_by_id, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = id[i];
+    const float m = m_by_id[k];
+    b.id[i] = k;
+    b.m[i] = m;
+    set_pos(b, i, x[i], y[i], z[i], m);
+}
+
+__global__ void k_mass_by_id(const BodyArrays b, float* m_by_id, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) m_by_id[b.id[i]] = b.m[i];
+}
+
+// Weights in the current body order from the id-indexed ones.
+__global__ void k_gather_w(const BodyArrays b, const float4* w_by_id, float4* w, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = w_by_id[b.id[i]];
+}
+
+// lx[id] += G g_x, ..., lm[id] += G g_m (g in the current body order).
+__global__ void k_tree_vjp_apply(const BodyArrays b, const double* g, int n, double G, double* lx, double* ly,
+                                 double* lz, double* lm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = b.id[i];
+    lx[k] += G * g[i];
+    ly[k] += G * g[n + i];
+    lz[k] += G * g[2 * static_cast<size_t>(n) + i];
+    lm[k] += G * g[3 * static_cast<size_t>(n) + i];
+}
+
+// Terminal adjoints indexed by id.
+__global__ void k_adj_init_id(const BodyArrays b, const double* tx, const double* ty, const double* tz, double* lx,
+                              double* ly, double* lz, double* lvx, double* lvy, double* lvz, double* lm,
+                              double* loss_terms, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = b.id[i];
+    const double m = b.m[i];
+    const double dx = b.x[i] - tx[id], dy = b.y[i] - ty[id], dz = b.z[i] - tz[id];
+    lx[id] = 2 * m * dx; ly[id] = 2 * m * dy; lz[id] = 2 * m * dz;
+    lvx[id] = lvy[id] = lvz[id] = 0;
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    lm[id] = d2;
+    loss_terms[id] = m * d2;
 }
 
 __global__ void k_copy_hilo(const BodyArrays b, float4* hm, float4* lo, int n) {
@@ -222,8 +293,10 @@ struct AdjointState {
     int n = 0, steps = 0, every = 0, nck = 0;
     double dt = 0;
     lg_force_params p{};
-    DevBuf ck_x, ck_y, ck_z, ck_vx, ck_vy, ck_vz;  // checkpoints, nck * n each
-    DevBuf seg_hm, seg_lo;                         // one segment's positions, (every + 1) * n float4
+    DevBuf ck_x, ck_y, ck_z, ck_vx, ck_vy, ck_vz, ck_m, ck_id;  // checkpoints, nck * n each
+    DevBuf seg_hm, seg_lo;                         // direct: one segment's positions, every * n float4
+    DevBuf seg_x, seg_y, seg_z, seg_id;            // tree: one segment's sorted FP64 positions and ids
+    DevBuf m_by_id, w_sorted, gbuf;                // tree: masses by id, weights in body order, VJP output
     DevBuf lx, ly, lz, lvx, lvy, lvz, lm, loss_terms, w, partial;
     DevBuf tx, ty, tz;
     bool have_forward = false;
@@ -243,7 +316,41 @@ void save_ck(Engine& e, AdjointState& a, int slot) {
     const size_t off = static_cast<size_t>(slot) * a.n;
     k_save<<<grid_for(a.n, 256), 256, 0, e.stream>>>(e.bodies(e.cur), a.ck_x.as<double>() + off, a.ck_y.as<double>() + off,
                                                    a.ck_z.as<double>() + off, a.ck_vx.as<float>() + off,
-                                                   a.ck_vy.as<float>() + off, a.ck_vz.as<float>() + off, a.n);
+                                                   a.ck_vy.as<float>() + off, a.ck_vz.as<float>() + off,
+                                                   a.ck_m.as<float>() + off, a.ck_id.as<uint32_t>() + off, a.n);
+    LG_LAUNCHED();
+    ++e.launches;
+}
+
+void restore_ck(Engine& e, AdjointState& a, int slot) {
+    const size_t off = static_cast<size_t>(slot) * a.n;
+    k_restore<<<grid_for(a.n, 256), 256, 0, e.stream>>>(e.bodies(e.cur), a.ck_x.as<double>() + off,
+                                                      a.ck_y.as<double>() + off, a.ck_z.as<double>() + off,
+                                                      a.ck_vx.as<float>() + off, a.ck_vy.as<float>() + off,
+                                                      a.ck_vz.as<float>() + off, a.ck_m.as<float>() + off,
+                                                      a.ck_id.as<uint32_t>() + off, a.n);
+    LG_LAUNCHED();
+    ++e.launches;
+}
+
+// Tree forces through the engine's own build and walk (sizes checked, as every force call).
+void tree_forces(Engine& e, const lg_force_params& p) {
+    e.build_tree(p);
+    e.compute_forces_with(p, false, 0);
+}
+
+void kdk_step_tree(Engine& e, const lg_force_params& p, double dt) {
+    e.kick(0.5 * dt);
+    e.drift(dt);
+    tree_forces(e, p);
+    e.kick(0.5 * dt);
+}
+
+void store_step(Engine& e, AdjointState& a, int slot) {
+    const size_t so = static_cast<size_t>(slot) * a.n;
+    k_store_step<<<grid_for(a.n, 256), 256, 0, e.stream>>>(e.bodies(e.cur), a.seg_x.as<double>() + so,
+                                                         a.seg_y.as<double>() + so, a.seg_z.as<double>() + so,
+                                                         a.seg_id.as<uint32_t>() + so, a.n);
     LG_LAUNCHED();
     ++e.launches;
 }
@@ -269,7 +376,8 @@ void kdk_step(Engine& e, const lg_force_params& p, double dt) {
 }  // namespace
 
 void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every) {
-    if (p.method != LG_DIRECT) fail(kRuntime, "adjoint: only the direct method is supported");
+    if (p.method != LG_DIRECT && p.method != LG_TREE) fail(kArg, "adjoint: unknown force method");
+    const bool tree = p.method == LG_TREE;
     if (steps < 1 || every < 1) fail(kArg, "adjoint: steps and checkpoint interval must be positive");
     LG_CK(cudaSetDevice(e.dev));
     const int n = e.n;
@@ -283,16 +391,32 @@ void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, doubl
     const size_t cn = static_cast<size_t>(a.nck) * n;
     a.ck_x.reserve(cn * 8); a.ck_y.reserve(cn * 8); a.ck_z.reserve(cn * 8);
     a.ck_vx.reserve(cn * 4); a.ck_vy.reserve(cn * 4); a.ck_vz.reserve(cn * 4);
-    direct_forces(e, p);
+    a.ck_m.reserve(cn * 4); a.ck_id.reserve(cn * 4);
+    if (tree) {
+        // Ids index the adjoint state: they must be a permutation of 0..n-1.
+        std::vector<uint32_t> ids(static_cast<size_t>(n));
+        LG_CK(cudaMemcpyAsync(ids.data(), e.bodies(e.cur).id, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost,
+                              e.stream));
+        LG_CK(cudaStreamSynchronize(e.stream));
+        std::vector<char> seen(static_cast<size_t>(n), 0);
+        for (uint32_t k : ids) {
+            if (k >= static_cast<uint32_t>(n) || seen[k]) fail(kArg, "adjoint (tree): body ids must be 0..n-1");
+            seen[k] = 1;
+        }
+        tree_forces(e, p);
+    } else {
+        direct_forces(e, p);
+    }
     save_ck(e, a, 0);
     for (int s = 0; s < steps; ++s) {
-        kdk_step(e, p, dt);
+        if (tree) kdk_step_tree(e, p, dt);
+        else kdk_step(e, p, dt);
         if ((s + 1) % every == 0 && s + 1 < steps) save_ck(e, a, (s + 1) / every);
     }
     e.acc_ok = true;
     e.has_pe = false;
-    e.tree_ok = false;
-    e.costs_ok = false;
+    e.tree_ok = tree;
+    e.costs_ok = tree;
     a.have_forward = true;
     LG_CK(cudaStreamSynchronize(e.stream));
     e.check_device_errors("adjoint forward");
@@ -303,51 +427,79 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     if (!a.have_forward || a.n != e.n) fail(kLogic, "adjoint backward: run the adjoint forward pass first");
     LG_CK(cudaSetDevice(e.dev));
     const int n = a.n;
+    const bool tree = a.p.method == LG_TREE;
     cudaStream_t s = e.stream;
     const size_t nb8 = static_cast<size_t>(n) * 8;
     for (DevBuf* d : {&a.lx, &a.ly, &a.lz, &a.lvx, &a.lvy, &a.lvz, &a.lm, &a.loss_terms, &a.tx, &a.ty, &a.tz})
         d->reserve(nb8);
     a.w.reserve(static_cast<size_t>(n) * 16);
-    a.seg_hm.reserve(static_cast<size_t>(a.every + 1) * n * 16);
-    a.seg_lo.reserve(static_cast<size_t>(a.every + 1) * n * 16);
+    const size_t seg_n = static_cast<size_t>(a.every) * n;
+    if (tree) {
+        a.seg_x.reserve(seg_n * 8); a.seg_y.reserve(seg_n * 8); a.seg_z.reserve(seg_n * 8);
+        a.seg_id.reserve(seg_n * 4);
+        a.m_by_id.reserve(static_cast<size_t>(n) * 4);
+        a.w_sorted.reserve(static_cast<size_t>(n) * 16);
+        a.gbuf.reserve(static_cast<size_t>(n) * 32);
+    } else {
+        a.seg_hm.reserve(seg_n * 16);
+        a.seg_lo.reserve(seg_n * 16);
+    }
     LG_CK(cudaMemcpyAsync(a.tx.as<double>(), tx, nb8, cudaMemcpyHostToDevice, s));
     LG_CK(cudaMemcpyAsync(a.ty.as<double>(), ty, nb8, cudaMemcpyHostToDevice, s));
     LG_CK(cudaMemcpyAsync(a.tz.as<double>(), tz, nb8, cudaMemcpyHostToDevice, s));
     const int gb = grid_for(n, 256);
-    // The forward pass left the final state resident: terminal adjoints from it.
-    k_adj_init<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
-                                  a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
-                                  a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(), a.loss_terms.as<double>(), n);
-    LG_LAUNCHED();
+    // The forward pass left the final state resident: terminal adjoints from it (by body index for
+    // the direct path, whose order never changes; by id for the tree path).
+    if (tree) {
+        k_adj_init_id<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
+                                         a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                         a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(),
+                                         a.loss_terms.as<double>(), n);
+        LG_LAUNCHED();
+        k_mass_by_id<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.m_by_id.as<float>(), n);
+        LG_LAUNCHED();
+    } else {
+        k_adj_init<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
+                                      a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                      a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(), a.loss_terms.as<double>(),
+                                      n);
+        LG_LAUNCHED();
+    }
     std::vector<double> terms(static_cast<size_t>(n));
     LG_CK(cudaMemcpyAsync(terms.data(), a.loss_terms.as<double>(), nb8, cudaMemcpyDeviceToHost, s));
-    // VJP launch shape: whole waves over split-j slices.
+    // Direct VJP launch shape: whole waves over split-j slices.
     const int iblocks = (n + VBS * VIPT - 1) / (VBS * VIPT);
     int slices = std::max(1, std::min(n / 128 + 1, (2 * e.sms + iblocks - 1) / iblocks));
     int jslice = (n + slices - 1) / slices;
     slices = (n + jslice - 1) / jslice;
-    a.partial.reserve(static_cast<size_t>(slices) * n * 16);
+    if (!tree) a.partial.reserve(static_cast<size_t>(slices) * n * 16);
     const float e2 = static_cast<float>(a.p.eps * a.p.eps);
     const bool eps0 = !(e2 >= 1.17549435e-38f);
     const double h = 0.5 * a.dt;
     for (int seg = (a.steps - 1) / a.every; seg >= 0; --seg) {
         const int s0 = seg * a.every, s1 = std::min(a.steps, s0 + a.every);
         // Restore the checkpoint at s0 and recompute the segment's positions.
-        const size_t off = static_cast<size_t>(seg) * n;
-        k_restore<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.ck_x.as<double>() + off, a.ck_y.as<double>() + off,
-                                     a.ck_z.as<double>() + off, a.ck_vx.as<float>() + off, a.ck_vy.as<float>() + off,
-                                     a.ck_vz.as<float>() + off, n);
-        LG_LAUNCHED();
-        direct_forces(e, a.p);
-        k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>(), a.seg_lo.as<float4>(), n);
-        LG_LAUNCHED();
-        for (int st = s0; st < s1 - 1; ++st) {
-            kdk_step(e, a.p, a.dt);
-            const size_t so = static_cast<size_t>(st - s0 + 1) * n;
-            k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, n);
+        restore_ck(e, a, seg);
+        if (tree) {
+            tree_forces(e, a.p);
+            store_step(e, a, 0);
+            for (int st = s0; st < s1 - 1; ++st) {
+                kdk_step_tree(e, a.p, a.dt);
+                store_step(e, a, st - s0 + 1);
+            }
+        } else {
+            direct_forces(e, a.p);
+            k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>(), a.seg_lo.as<float4>(), n);
             LG_LAUNCHED();
+            for (int st = s0; st < s1 - 1; ++st) {
+                kdk_step(e, a.p, a.dt);
+                const size_t so = static_cast<size_t>(st - s0 + 1) * n;
+                k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
+                                               n);
+                LG_LAUNCHED();
+            }
+            e.launches += 1 + (s1 - 1 - s0);
         }
-        e.launches += 2 + (s1 - 1 - s0);
         // Reverse through the segment.
         for (int st = s1 - 1; st >= s0; --st) {
             const double c = st > 0 ? a.dt : h;
@@ -355,18 +507,39 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
                                           a.lvy.as<double>(), a.lvz.as<double>(), a.dt, c, a.w.as<float4>(), n);
             LG_LAUNCHED();
             const size_t so = static_cast<size_t>(st - s0) * n;
-            dim3 grid(iblocks, slices);
-            if (eps0)
-                k_vjp<true><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, a.w.as<float4>(), n,
-                                                 jslice, e2, a.partial.as<float4>());
-            else
-                k_vjp<false><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so, a.w.as<float4>(),
-                                                  n, jslice, e2, a.partial.as<float4>());
-            LG_LAUNCHED();
-            k_vjp_apply<<<gb, 256, 0, s>>>(a.partial.as<float4>(), n, slices, a.p.G, a.lx.as<double>(), a.ly.as<double>(),
-                                           a.lz.as<double>(), a.lm.as<double>());
-            LG_LAUNCHED();
-            e.launches += 3;
+            if (tree) {
+                // The step's sorted positions, then an exact rebuild of its tree.
+                k_load_step<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_x.as<double>() + so, a.seg_y.as<double>() + so,
+                                               a.seg_z.as<double>() + so, a.seg_id.as<uint32_t>() + so,
+                                               a.m_by_id.as<float>(), n);
+                LG_LAUNCHED();
+                tree_reset_guess(e);
+                e.build_tree(a.p);
+                k_gather_w<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.w.as<float4>(), a.w_sorted.as<float4>(), n);
+                LG_LAUNCHED();
+                LG_CK(cudaMemsetAsync(a.gbuf.as<double>(), 0, static_cast<size_t>(n) * 32, s));
+                tree_walk_vjp(e, a.w_sorted.as<float4>(), e2, eps0, a.gbuf.as<double>());
+                k_tree_vjp_apply<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.gbuf.as<double>(), n, a.p.G, a.lx.as<double>(),
+                                                    a.ly.as<double>(), a.lz.as<double>(), a.lm.as<double>());
+                LG_LAUNCHED();
+                e.launches += 4;
+                LG_CK(cudaMemcpyAsync(e.pinned_small, e.err_word(), 4, cudaMemcpyDeviceToHost, s));
+                LG_CK(cudaStreamSynchronize(s));
+                e.check_device_errors("adjoint backward (tree VJP)");
+            } else {
+                dim3 grid(iblocks, slices);
+                if (eps0)
+                    k_vjp<true><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
+                                                     a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
+                else
+                    k_vjp<false><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
+                                                      a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
+                LG_LAUNCHED();
+                k_vjp_apply<<<gb, 256, 0, s>>>(a.partial.as<float4>(), n, slices, a.p.G, a.lx.as<double>(),
+                                               a.ly.as<double>(), a.lz.as<double>(), a.lm.as<double>());
+                LG_LAUNCHED();
+                e.launches += 3;
+            }
         }
     }
     // Gradients in id order.
@@ -381,13 +554,13 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     double* dst[7] = {gx, gy, gz, gvx, gvy, gvz, gm};
     for (int k = 0; k < 7; ++k)
         if (dst[k])
-            for (int i = 0; i < n; ++i) dst[k][ids[i]] = buf[static_cast<size_t>(k) * n + i];
+            for (int i = 0; i < n; ++i) dst[k][tree ? static_cast<uint32_t>(i) : ids[i]] = buf[static_cast<size_t>(k) * n + i];
     double L = 0;
     for (double t : terms) L += t;
-    // The backward pass restored and replayed segment 0 only in part: the resident state is the
-    // first segment's, so the forward result is no longer resident.
+    // The backward pass replayed the segments: the forward's final state is no longer resident.
     a.have_forward = false;
     e.acc_ok = false;
+    e.tree_ok = false;
     return L;
 }
 

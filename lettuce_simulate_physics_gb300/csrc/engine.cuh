@@ -25,6 +25,13 @@ struct TreeView {
     const float4* grp_box;    // 2 per group: (bx, by, bz, 0), (hx, hy, hz, 0)
     const unsigned* ngroups;  // device-side group count
     size_t T;
+    // For the walk's vector-Jacobian product: parent of every node (root: 0xffffffff), leaf of
+    // every body, node of every leaf.
+    const uint32_t* nd_parent;
+    const uint32_t* body_leaf;
+    const uint32_t* leaf_node;
+    const unsigned* nleaves;  // device-side leaf count
+    size_t K;
 };
 
 struct BodySet {
@@ -89,6 +96,7 @@ struct Engine {
     DevBuf diag_partial; // per-block FP64 partials
     DevBuf flush_buf;
     DevBuf walk_stack;   // per-warp traversal stacks of the tree walk
+    DevBuf vjp_scratch;  // per-node adjoints of the tree walk's vector-Jacobian product
     DevBuf small;        // error word, tickets, counters, FP64 results
     unsigned* pinned_small = nullptr;
     bool has_pe = false, acc_ok = true, tree_ok = false, costs_ok = false;
@@ -133,6 +141,16 @@ const void* probe_kernel();
 // sys/e2_sys: forest walk (per-body system, per-system squared softening); nullptr for one tree.
 void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys = nullptr,
                const float* e2_sys = nullptr);
+// walk_vjp.cu: vector-Jacobian product of the tree forces over the current tree's interaction
+// lists (the lists are those of the force walk on the same tree), with the cell moments
+// differentiated through the bodies: g (4 arrays of n doubles: x, y, z, m; current body order)
+// accumulates d(sum_i w_i . a_i / G)/d(x, m). w: float4 weights per body (current order).
+void tree_walk_vjp(Engine& e, const float4* w, float e2, bool eps0, double* g);
+// walk_vjp.cu: vector-Jacobian product of the tree forces over the current tree's interaction
+// lists (the lists are those of the force walk on the same tree), with the cell moments
+// differentiated through the bodies: g (4 arrays of n doubles: x, y, z, m; current body order)
+// accumulates d(sum_i w_i . a_i / G)/d(x, m). w: float4 weights per body (current order).
+void tree_walk_vjp(Engine& e, const float4* w, float e2, bool eps0, double* g);
 // adjoint.cu
 std::unique_ptr<AdjointState, void (*)(AdjointState*)> make_adjoint_state();
 void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every);

@@ -1565,6 +1565,11 @@ TreeView tree_view(Engine& e) {
     v.grp_box = t.grp_box.as<float4>();
     v.ngroups = t.counts.as<unsigned>() + 3;
     v.T = t.T;  // capacity the build was launched with (>= the node count)
+    v.nd_parent = t.nd_parent.as<uint32_t>();
+    v.body_leaf = t.leafid.as<uint32_t>();
+    v.leaf_node = t.leaf_node.as<uint32_t>();
+    v.nleaves = t.counts.as<unsigned>() + 1;
+    v.K = t.K;
     return v;
 }
 

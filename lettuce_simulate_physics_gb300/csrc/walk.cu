@@ -19,21 +19,19 @@
 // The interaction count per body is the list length minus its own entry; the reference CPU
 // backend counts that self entry, so its count exceeds this one by exactly N.
 #include "engine.cuh"
+#include "walk_common.cuh"
 
 namespace lg {
 
 namespace {
+
+using namespace walk;
 
 constexpr int WBS = 128;  // 4 warps per block
 #ifndef LG_WALK_MINB
 #define LG_WALK_MINB 4  // resident blocks per SM the register budget is sized for
 #endif
 constexpr int WARPS = WBS / 32;
-constexpr int SMALL_LEAF = 4;   // src/cpu_backend.cpp:29
-constexpr int SCAP = 16384;     // traversal stack entries per warp (global memory)
-constexpr int CL_CAP = 160, CL_FLUSH = 128;
-constexpr int RL_CAP = 96, RL_FLUSH = 64;
-constexpr int BR_FLUSH = 256;
 constexpr int CCH = 64;   // cells converted per chunk
 constexpr int BCH = 128;  // bodies converted per chunk
 constexpr int PASS = 128; // i-bodies per pass (4 per lane)
@@ -66,17 +64,6 @@ struct WalkArgs {
     const uint32_t* sys;
     const float* e2_sys;
 };
-
-__device__ __forceinline__ int warp_excl_scan(int v, int lane, int& total) {
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += t;
-    }
-    total = __shfl_sync(0xffffffffu, x, 31);
-    return x - v;
-}
 
 __device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
 
@@ -236,32 +223,13 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
         __syncwarp();
     }
     if (nr == 0) return;
-    // Prefix of range lengths (nr <= RL_CAP).
-    for (int r0 = 0; r0 < nr; r0 += 32) {
-        const int r = r0 + lane;
-        const int len = r < nr ? static_cast<int>(s.rlist[r].y) : 0;
-        int tot;
-        const int ex = warp_excl_scan(len, lane, tot);
-        const uint32_t base = r0 == 0 ? 0u : s.rpre[r0];
-        __syncwarp();
-        if (r < nr) s.rpre[r] = base + ex;
-        if (lane == 31) s.rpre[min(r0 + 32, nr)] = base + tot;
-        __syncwarp();
-    }
-    const int total = static_cast<int>(s.rpre[nr]);
+    const int total = range_prefix(s, nr, lane);
     for (int b0 = 0; b0 < total; b0 += BCH) {
         const int bc = min(BCH, total - b0);
         const int bc2 = (bc + 1) & ~1;
         for (int k = lane; k < bc2; k += 32) {
             if (k < bc) {
-                const uint32_t p = b0 + k;
-                int lo = 0, hi = nr;  // last r with rpre[r] <= p
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s.rpre[mid] <= p) lo = mid;
-                    else hi = mid;
-                }
-                const uint32_t j = s.rlist[lo].x + (p - s.rpre[lo]);
+                const uint32_t j = range_body(s, nr, b0 + k);
                 const float4 h = w.hm[j], l = w.lo[j];
                 s.bx[k] = (h.x - ox) + l.x;
                 s.by[k] = (h.y - oy) + l.y;
@@ -296,82 +264,11 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     for (int u = 0; u < IPT_MAX; ++u)
 #pragma unroll
         for (int f = 0; f < 8; ++f) s.ks[u][f][lane] = 0.f;
-    const unsigned lt = (1u << lane) - 1u;
     const uint32_t root = w.sys ? w.sys[gr.x] : 0u;
     const float e2 = w.e2_sys ? w.e2_sys[root] : w.e2;
-    int sp = 1;
-    if (lane == 0) stack[0] = root;
-    __syncwarp();
-    int nc = 0, nr = 0, nbr = 0;
     uint32_t list_len = 0, cells_len = 0;
-    bool overflow = false;
-    // Each node is visited at most once per pass; the cap stops a malformed tree.
-    const uint32_t max_iter = static_cast<uint32_t>(w.tv.T) + 64u;
-    uint32_t iter = 0;
-    for (;;) {
-        const bool done = sp == 0;
-        // One evaluation site: when the lists fill up, and once at the end.
-        if (done || nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
-            flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2);
-            list_len += nc + nbr;
-            cells_len += nc;
-            nc = nr = nbr = 0;
-            if (done) break;
-        }
-        if (++iter > max_iter) {
-            overflow = true;
-            break;
-        }
-        const int take = min(32, sp);
-        sp -= take;
-        const bool have = lane < take;
-        const uint32_t node = have ? stack[sp + lane] : 0u;
-        __syncwarp();
-        int kind = 0;  // 1 cell, 2 bodies, 3 children
-        uint32_t a0 = 0, a1 = 0;
-        if (have && node >= w.tv.T) {
-            atomicOr(w.err, kErrNodeOverflow);
-        } else if (have) {
-            const uint4 r = w.tv.nd_range[node];
-            const float4 com = w.tv.nd_com[node];
-            const float rc2 = w.tv.nd_q1[node].z;
-            const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.x, bc.x)), bh.x), 0.f);
-            const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.y, bc.y)), bh.y), 0.f);
-            const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.z, bc.z)), bh.z), 0.f);
-            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            // A node containing the group is always opened (src/cpu_backend.cpp:826-828).
-            const bool contains = r.x <= gr.x && gr.y <= r.y;
-            const bool leaf = r.w == 0;
-            if (!contains && d2 >= rc2) {
-                if (leaf && r.y - r.x <= static_cast<unsigned>(SMALL_LEAF)) { kind = 2; a0 = r.x; a1 = r.y - r.x; }
-                else { kind = 1; a0 = node; }
-            } else if (leaf) {
-                kind = 2; a0 = r.x; a1 = r.y - r.x;
-            } else {
-                kind = 3; a0 = r.z; a1 = r.w;
-            }
-        }
-        const unsigned cm = __ballot_sync(0xffffffffu, kind == 1);
-        if (kind == 1) s.clist[nc + __popc(cm & lt)] = a0;
-        nc += __popc(cm);
-        const unsigned rm = __ballot_sync(0xffffffffu, kind == 2);
-        if (kind == 2) s.rlist[nr + __popc(rm & lt)] = make_uint2(a0, a1);
-        nr += __popc(rm);
-        int btot;
-        warp_excl_scan(kind == 2 ? static_cast<int>(a1) : 0, lane, btot);
-        nbr += btot;
-        int ctot;
-        const int coff = warp_excl_scan(kind == 3 ? static_cast<int>(a1) : 0, lane, ctot);
-        if (sp + ctot > SCAP) {
-            overflow = true;
-            break;
-        }
-        if (kind == 3)
-            for (uint32_t k = 0; k < a1; ++k) stack[sp + coff + k] = a0 + (a1 - 1 - k);  // first child on top
-        sp += ctot;
-        __syncwarp();
-    }
-    if (overflow && lane == 0) atomicOr(w.err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
+    traverse(w.tv, s, stack, lane, gr, bc, bh, root, w.err, list_len, cells_len,
+             [&](int nc, int nr) { flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2); });
     const float self_inv = (POT && !EPS0) ? rsqrt_mufu(e2) : 0.f;
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {

@@ -983,3 +983,225 @@ double or_adjoint_direct_fp64(size_t n, const double* x0, const double* v0, cons
     free(traj); free(x); free(v); free(w);
     return L;
 }
+
+/* ---- FP64 tree forces over frozen interaction lists --------------------------------------------
+ * Test oracle of the engine's tree adjoint (no reference counterpart). For every force call of a
+ * trajectory the caller passes the tree the engine built: its sorted body order (position -> id),
+ * node ranges and children (the reference node layout), the FP32 centres of mass and rcrit2 its
+ * opening test used, and the walk groups with their boxes. The interaction lists are rebuilt with
+ * the walk's opening rule (src/cpu_backend.cpp:816-838) in the same FP32 arithmetic, so they are
+ * the engine's lists; the forces then use them in FP64 with every cell's moments recomputed from
+ * the current positions (M = sum m, com = sum m x / M, Q = sum m (3 e e^T - |e|^2 I)):
+ *   a_i = G [sum_cells M d/r^3 - Q d/r^5 + 5/2 (d.Q.d) d/r^7 + sum_bodies m_j d/r^3],
+ *   d = X - x_i, r^2 = |d|^2 + eps^2.
+ * or_frozen_loss runs the KDK steps with the step-s lists at force call s and returns
+ * L = sum m |x_T - x*|^2; central differences of it check the engine's adjoint. */
+typedef struct {
+    uint32_t nn, ng;
+    uint32_t* range4;    /* 4 per node */
+    uint32_t* perm;      /* n */
+    uint32_t* glohi;     /* 2 per group */
+    uint32_t* coff;      /* ng + 1: cells of group g at cells[coff[g] .. coff[g+1]) */
+    uint32_t* cells;
+    uint32_t* boff;      /* ng + 1: body ranges of group g at branges[2 boff[g] ..) */
+    uint32_t* branges;
+} fz_step;
+
+struct or_frozen {
+    size_t n;
+    int steps;
+    fz_step* st;
+};
+
+typedef struct {
+    uint32_t* p;
+    size_t n, cap;
+} u32vec;
+
+static void u32_push(u32vec* v, uint32_t x) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 256;
+        v->p = realloc(v->p, v->cap * 4);
+        if (!v->p) abort();
+    }
+    v->p[v->n++] = x;
+}
+
+or_frozen* or_frozen_create(size_t n, int steps, const uint32_t* nn, const uint32_t* ng, const uint32_t* perm_all,
+                            const uint32_t* range4_all, const float* comrc_all, const uint32_t* glohi_all,
+                            const float* gbox_all) {
+    or_frozen* f = calloc(1, sizeof(or_frozen));
+    if (!f) abort();
+    f->n = n;
+    f->steps = steps;
+    f->st = calloc((size_t)steps, sizeof(fz_step));
+    if (!f->st) abort();
+    size_t no = 0, go = 0;
+    for (int s = 0; s < steps; ++s) {
+        fz_step* t = &f->st[s];
+        t->nn = nn[s];
+        t->ng = ng[s];
+        t->range4 = malloc((size_t)t->nn * 16);
+        t->perm = malloc(n * 4);
+        t->glohi = malloc((size_t)t->ng * 8);
+        t->coff = malloc(((size_t)t->ng + 1) * 4);
+        t->boff = malloc(((size_t)t->ng + 1) * 4);
+        if (!t->range4 || !t->perm || !t->glohi || !t->coff || !t->boff) abort();
+        memcpy(t->range4, range4_all + 4 * no, (size_t)t->nn * 16);
+        memcpy(t->perm, perm_all + (size_t)s * n, n * 4);
+        memcpy(t->glohi, glohi_all + 2 * go, (size_t)t->ng * 8);
+        const float* crc = comrc_all + 4 * no;
+        const float* gbox = gbox_all + 6 * go;
+        u32vec cells = {0}, br = {0}, stack = {0};
+        for (uint32_t g = 0; g < t->ng; ++g) {
+            t->coff[g] = (uint32_t)cells.n;
+            t->boff[g] = (uint32_t)(br.n / 2);
+            const uint32_t glo = t->glohi[2 * g], ghi = t->glohi[2 * g + 1];
+            const float bx = gbox[6 * g], by = gbox[6 * g + 1], bz = gbox[6 * g + 2];
+            const float hx = gbox[6 * g + 3], hy = gbox[6 * g + 4], hz = gbox[6 * g + 5];
+            stack.n = 0;
+            u32_push(&stack, 0);
+            while (stack.n) {
+                const uint32_t nd = stack.p[--stack.n];
+                const uint32_t* r = t->range4 + 4 * nd;
+                const float* c = crc + 4 * nd;
+                const float dx = fmaxf(fabsf(c[0] - bx) - hx, 0.f);
+                const float dy = fmaxf(fabsf(c[1] - by) - hy, 0.f);
+                const float dz = fmaxf(fabsf(c[2] - bz) - hz, 0.f);
+                const float d2 = (dx * dx + dy * dy) + dz * dz;
+                const int contains = r[0] <= glo && ghi <= r[1];
+                const int leaf = r[3] == 0;
+                if (!contains && d2 >= c[3]) {
+                    if (leaf && r[1] - r[0] <= 4) { u32_push(&br, r[0]); u32_push(&br, r[1]); }
+                    else u32_push(&cells, nd);
+                } else if (leaf) {
+                    u32_push(&br, r[0]); u32_push(&br, r[1]);
+                } else {
+                    for (uint32_t k = 0; k < r[3]; ++k) u32_push(&stack, r[2] + k);
+                }
+            }
+        }
+        t->coff[t->ng] = (uint32_t)cells.n;
+        t->boff[t->ng] = (uint32_t)(br.n / 2);
+        t->cells = cells.p;
+        t->branges = br.p;
+        free(stack.p);
+        no += t->nn;
+        go += t->ng;
+    }
+    return f;
+}
+
+void or_frozen_destroy(or_frozen* f) {
+    if (!f) return;
+    for (int s = 0; s < f->steps; ++s) {
+        fz_step* t = &f->st[s];
+        free(t->range4); free(t->perm); free(t->glohi); free(t->coff); free(t->cells); free(t->boff);
+        free(t->branges);
+    }
+    free(f->st);
+    free(f);
+}
+
+/* Forces of force call s at positions x (3 per id), masses m (per id). */
+static void frozen_accel(const or_frozen* f, int s, const double* x, const double* m, double G, double e2, double* a,
+                         double* mom /* 10 per node */, int nt) {
+    const fz_step* t = &f->st[s];
+    const long nn = (long)t->nn;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+    for (long c = 0; c < nn; ++c) {
+        const uint32_t lo = t->range4[4 * c], hi = t->range4[4 * c + 1];
+        double M = 0, sx = 0, sy = 0, sz = 0;
+        for (uint32_t p = lo; p < hi; ++p) {
+            const uint32_t j = t->perm[p];
+            M += m[j]; sx += m[j] * x[3 * j]; sy += m[j] * x[3 * j + 1]; sz += m[j] * x[3 * j + 2];
+        }
+        const double cx = M > 0 ? sx / M : 0, cy = M > 0 ? sy / M : 0, cz = M > 0 ? sz / M : 0;
+        double q[6] = {0, 0, 0, 0, 0, 0};
+        for (uint32_t p = lo; p < hi; ++p) {
+            const uint32_t j = t->perm[p];
+            const double ex = x[3 * j] - cx, ey = x[3 * j + 1] - cy, ez = x[3 * j + 2] - cz;
+            const double r2 = ex * ex + ey * ey + ez * ez;
+            q[0] += m[j] * (3 * ex * ex - r2); q[1] += m[j] * 3 * ex * ey; q[2] += m[j] * 3 * ex * ez;
+            q[3] += m[j] * (3 * ey * ey - r2); q[4] += m[j] * 3 * ey * ez; q[5] += m[j] * (3 * ez * ez - r2);
+        }
+        double* o = mom + 10 * c;
+        o[0] = M; o[1] = cx; o[2] = cy; o[3] = cz;
+        for (int k = 0; k < 6; ++k) o[4 + k] = q[k];
+    }
+    const long ng = (long)t->ng;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 4)
+    for (long g = 0; g < ng; ++g) {
+        for (uint32_t p = t->glohi[2 * g]; p < t->glohi[2 * g + 1]; ++p) {
+            const uint32_t i = t->perm[p];
+            const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+            double ax = 0, ay = 0, az = 0;
+            for (uint32_t k = t->coff[g]; k < t->coff[g + 1]; ++k) {
+                const double* o = mom + 10 * t->cells[k];
+                const double dx = o[1] - xi, dy = o[2] - yi, dz = o[3] - zi;
+                const double r2 = dx * dx + dy * dy + dz * dz + e2;
+                const double inv = 1 / sqrt(r2), inv2 = inv * inv, inv3 = inv * inv2, inv5 = inv3 * inv2;
+                const double inv7 = inv5 * inv2;
+                const double qx = o[4] * dx + o[5] * dy + o[6] * dz;
+                const double qy = o[5] * dx + o[7] * dy + o[8] * dz;
+                const double qz = o[6] * dx + o[8] * dy + o[9] * dz;
+                const double dqd = dx * qx + dy * qy + dz * qz;
+                const double fr = o[0] * inv3 + 2.5 * dqd * inv7;
+                ax += fr * dx - qx * inv5;
+                ay += fr * dy - qy * inv5;
+                az += fr * dz - qz * inv5;
+            }
+            for (uint32_t k = t->boff[g]; k < t->boff[g + 1]; ++k) {
+                for (uint32_t q = t->branges[2 * k]; q < t->branges[2 * k + 1]; ++q) {
+                    const uint32_t j = t->perm[q];
+                    if (j == i) continue;
+                    const double dx = x[3 * j] - xi, dy = x[3 * j + 1] - yi, dz = x[3 * j + 2] - zi;
+                    const double r2 = dx * dx + dy * dy + dz * dz + e2;
+                    if (!(r2 > 0)) continue;
+                    const double inv = 1 / sqrt(r2), fr = m[j] * inv * inv * inv;
+                    ax += fr * dx; ay += fr * dy; az += fr * dz;
+                }
+            }
+            a[3 * i] = G * ax; a[3 * i + 1] = G * ay; a[3 * i + 2] = G * az;
+        }
+    }
+}
+
+double or_frozen_loss(const or_frozen* f, const double* x0, const double* v0, const double* m, double G, double eps,
+                      double dt, const double* xstar, int threads) {
+    const int nt = threads > 0 ? threads : omp_get_max_threads();
+    const size_t n = f->n, n3 = 3 * n;
+    uint32_t maxnn = 1;
+    for (int s = 0; s < f->steps; ++s) maxnn = f->st[s].nn > maxnn ? f->st[s].nn : maxnn;
+    double* x = malloc(n3 * 8);
+    double* v = malloc(n3 * 8);
+    double* a = malloc(n3 * 8);
+    double* mom = malloc((size_t)maxnn * 80);
+    if (!x || !v || !a || !mom) abort();
+    memcpy(x, x0, n3 * 8);
+    memcpy(v, v0, n3 * 8);
+    const double e2 = eps * eps, h = 0.5 * dt;
+    frozen_accel(f, 0, x, m, G, e2, a, mom, nt);
+    for (int s = 0; s < f->steps; ++s) {
+        for (size_t k = 0; k < n3; ++k) v[k] += h * a[k];
+        for (size_t k = 0; k < n3; ++k) x[k] += dt * v[k];
+        if (s + 1 < f->steps) {
+            frozen_accel(f, s + 1, x, m, G, e2, a, mom, nt);
+            for (size_t k = 0; k < n3; ++k) v[k] += h * a[k];
+        }
+    }
+    const double L = loss_of((long)n, x, m, xstar);
+    free(x); free(v); free(a); free(mom);
+    return L;
+}
+
+/* Accelerations of force call s at positions x (3 per id) over its frozen lists (3 per id out). */
+void or_frozen_accel(const or_frozen* f, int s, const double* x, const double* m, double G, double eps, double* a,
+                     int threads) {
+    const int nt = threads > 0 ? threads : omp_get_max_threads();
+    uint32_t nn = f->st[s].nn ? f->st[s].nn : 1;
+    double* mom = malloc((size_t)nn * 80);
+    if (!mom) abort();
+    frozen_accel(f, s, x, m, G, eps * eps, a, mom, nt);
+    free(mom);
+}

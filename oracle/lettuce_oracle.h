@@ -90,6 +90,21 @@ double or_adjoint_direct_fp64(size_t n, const double* x0, const double* v0, cons
 double or_loss_direct_fp64(size_t n, const double* x0, const double* v0, const double* m, double G, double eps,
                            double dt, int steps, const double* xstar, int threads);
 
+/* FP64 tree forces over frozen interaction lists (test oracle of the engine's tree adjoint): one
+ * entry per force call of a trajectory of `steps` steps; per call s: nn[s] nodes (range4: lo, hi,
+ * first, nchild; comrc: FP32 cx, cy, cz, rcrit2), ng[s] groups (glohi; gbox: bx, by, bz, hx, hy,
+ * hz), perm: sorted position -> id (n per call). Arrays of all calls back to back. */
+typedef struct or_frozen or_frozen;
+or_frozen* or_frozen_create(size_t n, int steps, const uint32_t* nn, const uint32_t* ng, const uint32_t* perm_all,
+                            const uint32_t* range4_all, const float* comrc_all, const uint32_t* glohi_all,
+                            const float* gbox_all);
+void or_frozen_destroy(or_frozen* f);
+/* L = sum m |x_T - x*|^2 after the KDK steps (x0, v0, xstar: 3 per id; m per id). */
+double or_frozen_loss(const or_frozen* f, const double* x0, const double* v0, const double* m, double G, double eps,
+                      double dt, const double* xstar, int threads);
+void or_frozen_accel(const or_frozen* f, int s, const double* x, const double* m, double G, double eps, double* a,
+                     int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,6 +106,14 @@ def _lib(kind: str) -> C.CDLL:
         lib.or_loss_direct_fp64.restype = C.c_double
         lib.or_loss_direct_fp64.argtypes = [C.c_size_t, _d, _d, _d, C.c_double, C.c_double, C.c_double, C.c_int,
                                             _d, C.c_int]
+        lib.or_frozen_create.restype = vp
+        lib.or_frozen_create.argtypes = [C.c_size_t, C.c_int, _u, _u, _u, _u, _f, _u, _f]
+        lib.or_frozen_destroy.restype = None
+        lib.or_frozen_destroy.argtypes = [vp]
+        lib.or_frozen_loss.restype = C.c_double
+        lib.or_frozen_loss.argtypes = [vp, _d, _d, _d, C.c_double, C.c_double, C.c_double, _d, C.c_int]
+        lib.or_frozen_accel.restype = None
+        lib.or_frozen_accel.argtypes = [vp, C.c_int, _d, _d, C.c_double, C.c_double, _d, C.c_int]
     _libs[kind] = lib
     return lib
 
@@ -270,6 +278,57 @@ def loss_direct_fp64(x0, v0, m, G, eps, dt, steps, xstar, threads=0):
     xstar = np.ascontiguousarray(xstar, np.float64)
     return lib.or_loss_direct_fp64(m.shape[0], _dp(x0), _dp(v0), _dp(m), float(G), float(eps), float(dt),
                                    int(steps), _dp(xstar), int(threads))
+
+
+class FrozenTree:
+    """FP64 tree forces over frozen interaction lists for a trajectory (or_frozen_*): `calls` is a
+    list, one per force call s = 0 .. steps-1, of dicts with the engine's tree after that call:
+    perm (sorted position -> id), range4 (nn, 4), moments11 (nn, 11: cx cy cz m q.. rcrit2),
+    glohi (ng, 2), box6 (ng, 6). loss(x0, v0, m, xstar) runs the KDK steps in FP64 with those lists
+    and cell moments recomputed from the positions."""
+
+    def __init__(self, n, calls):
+        lib = _lib("port")
+        self._lib = lib
+        self.n = int(n)
+        self.steps = len(calls)
+        nn = np.array([len(c["range4"]) for c in calls], np.uint32)
+        ng = np.array([len(c["glohi"]) for c in calls], np.uint32)
+        perm = np.ascontiguousarray(np.concatenate([np.asarray(c["perm"], np.uint32) for c in calls]))
+        r4 = np.ascontiguousarray(np.concatenate([np.asarray(c["range4"], np.uint32).reshape(-1) for c in calls]))
+        crc = np.ascontiguousarray(np.concatenate(
+            [np.asarray(c["moments11"], np.float32)[:, [0, 1, 2, 10]].reshape(-1) for c in calls]))
+        gl = np.ascontiguousarray(np.concatenate([np.asarray(c["glohi"], np.uint32).reshape(-1) for c in calls]))
+        gb = np.ascontiguousarray(np.concatenate([np.asarray(c["box6"], np.float32).reshape(-1) for c in calls]))
+        self._h = lib.or_frozen_create(self.n, self.steps, _up(nn), _up(ng), _up(perm), _up(r4), _fp(crc), _up(gl),
+                                       _fp(gb))
+
+    def loss(self, x0, v0, m, G, eps, dt, xstar, threads=0):
+        x0 = np.ascontiguousarray(x0, np.float64)
+        v0 = np.ascontiguousarray(v0, np.float64)
+        m = np.ascontiguousarray(m, np.float64)
+        xstar = np.ascontiguousarray(xstar, np.float64)
+        return self._lib.or_frozen_loss(self._h, _dp(x0), _dp(v0), _dp(m), float(G), float(eps), float(dt),
+                                        _dp(xstar), int(threads))
+
+    def accel(self, s, x, m, G, eps, threads=0):
+        """(n, 3) FP64 accelerations of force call s at positions x (n, 3) by id."""
+        x = np.ascontiguousarray(x, np.float64)
+        m = np.ascontiguousarray(m, np.float64)
+        a = np.zeros((self.n, 3))
+        self._lib.or_frozen_accel(self._h, int(s), _dp(x), _dp(m), float(G), float(eps), _dp(a), int(threads))
+        return a
+
+    def close(self):
+        if self._h:
+            self._lib.or_frozen_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 if __name__ == "__main__":

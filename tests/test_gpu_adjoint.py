@@ -1,9 +1,16 @@
-"""Adjoint of the KDK leapfrog (direct forces) on the GPU, through the C ABI, against the FP64 CPU
-adjoint (oracle/lettuce_oracle.c) and FP64 central finite differences of the FP64 loss (h = 1e-5).
+"""Adjoint of the KDK leapfrog on the GPU, through the C ABI.
 
-Stated tolerances: loss within 1e-6 relative of the FP64 forward; gradient arrays within 1e-4
-relative (norm of the difference over the norm) of the FP64 adjoint; sampled components within
-1e-4 relative of the FP64 central differences (FP32 pair arithmetic in the forward and the VJP)."""
+Direct forces: against the FP64 CPU adjoint (oracle/lettuce_oracle.c) and FP64 central finite
+differences of the FP64 loss (h = 1e-5). Stated tolerances: loss within 1e-6 relative of the FP64
+forward; gradient arrays within 1e-4 relative (norm of the difference over the norm) of the FP64
+adjoint; sampled components within 1e-4 relative of the FP64 central differences (FP32 pair
+arithmetic in the forward and the VJP).
+
+Tree forces (frozen interaction lists): against FP64 central differences of the FP64 frozen-list
+loss (oracle FrozenTree: the engine's own trees of the trajectory, lists rebuilt with the walk's
+opening rule, cell moments recomputed from the perturbed positions). Stated tolerances: sampled
+components within 1e-3 relative (+1e-6 of the largest component), a random directional derivative
+within 1e-4 relative; at theta = 0 the tree adjoint equals the direct adjoint within 1e-5."""
 import numpy as np
 import pytest
 
@@ -73,5 +80,97 @@ def test_adjoint_backward_requires_forward(be):
     be.upload(b)
     with pytest.raises(L.LogicError):
         be.adjoint_backward(b.pos64())
-    with pytest.raises(RuntimeError):
+    bad = b.copy()
+    bad.id = bad.id + 5
+    be.upload(bad)
+    with pytest.raises(ValueError):  # the tree path indexes its adjoint state by id
         be.adjoint_forward(L.ForceParams(eps=0.05, method=L.ForceMethod.tree), 1e-3, 4, 2)
+
+
+def _tree_record(be):
+    """The engine's tree after a force call, as a frozen-list record for the oracle."""
+    r, mo, _ = be.tree_nodes()
+    box, lohi = be.tree_groups()
+    return {"perm": be.download().id.astype(np.uint32), "range4": r, "moments11": mo, "glohi": lohi, "box6": box}
+
+
+def _by_id(be, cols):
+    ids = be.download().id
+    out = np.zeros((len(ids), cols.shape[0]))
+    out[ids] = cols.T
+    return out
+
+
+def test_tree_adjoint_theta0_equals_direct_adjoint(be):
+    """At theta = 0 every list is all bodies: the tree VJP is the pairwise VJP."""
+    b = S.plummer(600, 6, cut=10)
+    G, eps, dt, steps, every = 1.0, 0.03, 1e-3, 12, 4
+    rng = np.random.Generator(np.random.PCG64(6))
+    xstar = b.pos64() + rng.normal(0, 1e-2, (len(b), 3))
+    out = []
+    for method in (L.ForceMethod.direct, L.ForceMethod.tree):
+        be.upload(b)
+        be.adjoint_forward(L.ForceParams(G=G, eps=eps, theta=0.0, method=method), dt, steps, every)
+        out.append(be.adjoint_backward(xstar))
+    (ld, gxd, gvd, gmd), (lt, gxt, gvt, gmt) = out
+    assert abs(lt / ld - 1) <= 1e-6
+    assert _rel(gxt, gxd) <= 1e-5 and _rel(gvt, gvd) <= 1e-5 and _rel(gmt, gmd) <= 1e-5
+
+
+@pytest.mark.parametrize("theta", [0.6, 0.3])
+def test_tree_adjoint_vs_frozen_list_central_differences(be, theta):
+    b = S.plummer(3000, 4, cut=10)
+    n = len(b)
+    G, eps, dt, steps, every = 1.0, 0.02, 2e-3, 6, 2
+    p = L.ForceParams(G=G, eps=eps, theta=theta, method=L.ForceMethod.tree)
+    # The trajectory's trees through the plain API (the adjoint's forward runs the same kernels).
+    be.upload(b)
+    be.compute_forces(p, False)
+    calls = [_tree_record(be)]
+    for s in range(steps):
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        if s + 1 < steps:
+            calls.append(_tree_record(be))
+        be.kick(0.5 * dt)
+    xT = _by_id(be, be.pos64())
+    rng = np.random.Generator(np.random.PCG64(7))
+    xstar = xT + rng.normal(0, 1e-2, xT.shape)
+    be.upload(b)
+    be.adjoint_forward(p, dt, steps, every)
+    assert np.array_equal(_by_id(be, be.pos64()), xT)  # bit-identical trajectory
+    loss, gx, gv, gm = be.adjoint_backward(xstar)
+    x0, v0, m = b.pos64(), b.vel64(), b.m.astype(np.float64)
+    fz = O.FrozenTree(n, calls)
+    L0 = fz.loss(x0, v0, m, G, eps, dt, xstar)
+    assert abs(loss / L0 - 1) <= 1e-5, (loss, L0)
+    h = 1e-5
+    worst = 0.0
+    for k, i in enumerate(rng.choice(n, size=8, replace=False)):
+        c = k % 3
+        for arr, grad in ((x0, gx), (v0, gv)):
+            pp, qq = arr.copy(), arr.copy()
+            pp[i, c] += h
+            qq[i, c] -= h
+            args_p = (pp, v0) if arr is x0 else (x0, pp)
+            args_q = (qq, v0) if arr is x0 else (x0, qq)
+            fd = (fz.loss(*args_p, m, G, eps, dt, xstar) - fz.loss(*args_q, m, G, eps, dt, xstar)) / (2 * h)
+            err = abs(grad[i, c] - fd) / (abs(fd) + 1e-3 * np.abs(grad).max())
+            worst = max(worst, err)
+            assert abs(grad[i, c] - fd) <= 1e-3 * abs(fd) + 1e-6 * np.abs(grad).max(), (i, c, grad[i, c], fd)
+        pm, qm = m.copy(), m.copy()
+        pm[i] += h * m[i]
+        qm[i] -= h * m[i]
+        fd = (fz.loss(x0, v0, pm, G, eps, dt, xstar) - fz.loss(x0, v0, qm, G, eps, dt, xstar)) / (2 * h * m[i])
+        assert abs(gm[i] - fd) <= 1e-3 * abs(fd) + 1e-6 * np.abs(gm).max(), (i, gm[i], fd)
+    # A random direction through every component.
+    dx, dv = rng.normal(0, 1, x0.shape), rng.normal(0, 1, v0.shape)
+    dm = rng.normal(0, 1, n) * m
+    hh = 1e-6
+    fd = (fz.loss(x0 + hh * dx, v0 + hh * dv, m + hh * dm, G, eps, dt, xstar)
+          - fz.loss(x0 - hh * dx, v0 - hh * dv, m - hh * dm, G, eps, dt, xstar)) / (2 * hh)
+    ad = float((gx * dx).sum() + (gv * dv).sum() + (gm * dm).sum())
+    print(f"theta={theta}: directional {ad:.9e} vs FD {fd:.9e}; worst sampled {worst:.2e}")
+    assert abs(ad - fd) <= 1e-4 * abs(fd), (ad, fd)
+    fz.close()

@@ -157,3 +157,53 @@ def test_fp64_adjoint_matches_central_differences():
         fd = (O.loss_direct_fp64(x0, v0, p, G, eps, dt, steps, xstar)
               - O.loss_direct_fp64(x0, v0, q, G, eps, dt, steps, xstar)) / (2 * h)
         assert abs(fd - gm[k]) <= 1e-6 * max(abs(fd), 1e-12) + 1e-12, (k, fd, gm[k])
+
+
+def _port_call(b, theta, eps):
+    """The port's tree after one force call, as a frozen-list record (perm, nodes, groups)."""
+    ob = O.OracleBackend("port")
+    ob.upload(b)
+    ob.compute_forces(O.TREE, 1.0, eps, theta, False)
+    out = ob.download()
+    nd = ob.nodes()
+    gr = ob.groups()
+    a = ob.accel()
+    ob.close()
+    call = {"perm": out.id.astype(np.uint32),
+            "range4": np.stack([nd["lo"], nd["hi"], nd["first"], nd["nchild"]], 1).astype(np.uint32),
+            "moments11": np.stack([nd[k] for k in ("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz",
+                                                   "rcrit2")], 1).astype(np.float32),
+            "glohi": np.stack([gr["lo"], gr["hi"]], 1).astype(np.uint32),
+            "box6": np.stack([gr[k] for k in ("bx", "by", "bz", "hx", "hy", "hz")], 1).astype(np.float32)}
+    acc = np.zeros((len(out), 3))
+    acc[out.id] = a[:3].T
+    return call, acc
+
+
+def test_frozen_lists_match_the_port_tree():
+    """The frozen-list oracle rebuilds the walk's lists from a tree and evaluates them in FP64: at
+    the tree's own positions it reproduces the port's FP32 tree forces."""
+    b = S.plummer(3000, 11, cut=20)
+    eps = 0.02
+    call, acc = _port_call(b, 0.6, eps)
+    fz = O.FrozenTree(len(b), [call])
+    x = np.stack([b.x, b.y, b.z], 1).astype(np.float64)
+    a64 = fz.accel(0, x, b.m, 1.0, eps)
+    assert rel_rms(acc.T, a64.T) <= 2e-6
+    fz.close()
+
+
+def test_frozen_lists_at_theta0_are_the_direct_sum():
+    """With theta = 0 every list is all bodies: the frozen-list loss equals the FP64 direct loss."""
+    b = S.plummer(700, 12, cut=20)
+    eps, dt, steps = 0.02, 2e-3, 3
+    call, _ = _port_call(b, 0.0, eps)
+    fz = O.FrozenTree(len(b), [call] * steps)
+    x0 = np.stack([b.x, b.y, b.z], 1).astype(np.float64)
+    v0 = np.stack([b.vx, b.vy, b.vz], 1).astype(np.float64)
+    rng = np.random.Generator(np.random.PCG64(1))
+    xs = x0 + rng.normal(0, 0.01, x0.shape)
+    L1 = fz.loss(x0, v0, b.m, 1.0, eps, dt, xs)
+    L2 = O.loss_direct_fp64(x0, v0, b.m, 1.0, eps, dt, steps, xs)
+    assert abs(L1 - L2) <= 1e-12 * abs(L2)
+    fz.close()
