@@ -314,6 +314,111 @@ def ensemble_leg(L, local, steps=200, seq_steps=10, count=512):
     }
 
 
+def collision_leg(L, local, n_each=8_000_000, steps=500, adj_steps=64, every=8, radius=2.0, width=0.05, h=0.5):
+    """Configuration 4: two inclined disks (each the disk1m recipe at n_each bodies) on a parabolic
+    approach; tree theta 0.6, eps 0.005, dt 5e-4; `steps` plain KDK steps, the last `adj_steps` of
+    them run as an adjoint window (frozen interaction lists, checkpoints every `every`). Loss: the
+    disk-1 mass within `radius` of the disk-1 core at the end, smoothed with a logistic step of
+    `width`; its gradient with respect to the disks' relative velocity at the start of the window
+    (disk 1 moves by f1 dv, disk 2 by -f0 dv, f = mass fractions). The adjoint is checked against
+    central differences of plain runs along the gradient with respect to all window-start
+    velocities."""
+    from lettuce_simulate_physics_gb300 import scenarios as S
+    t0 = time.perf_counter()
+    b, ne = S.collision(n_each)
+    gen_s = time.perf_counter() - t0
+    n = len(b)
+    p = L.ForceParams(G=1.0, eps=0.005, theta=0.6, method=L.ForceMethod.tree)
+    dt = 5e-4
+    be = L.CudaBackend(local)
+    be.upload(b)
+    be.compute_forces(p, False)
+    be.synchronize()
+    pre = steps - adj_steps
+    be.event_record(10)
+    for _ in range(pre):
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        be.kick(0.5 * dt)
+    be.event_record(11)
+    fwd_ms = be.event_elapsed(10, 11) / max(pre, 1)
+    bw = be.download()  # start of the adjoint window (positions rounded to float)
+    m1 = float(bw.m[bw.id < ne].sum())
+    m2 = float(bw.m[bw.id >= ne].sum())
+    f1, f0 = m2 / (m1 + m2), m1 / (m1 + m2)
+    d1 = np.zeros(n, bool)
+    d1[:ne] = True
+
+    def loss_and_seed(pos_by_id, m_by_id):
+        c = pos_by_id[0]
+        d = pos_by_id - c
+        r = np.sqrt((d * d).sum(1))
+        z = (radius - r) / width
+        sig = 1.0 / (1.0 + np.exp(-z))
+        Lv = float((m_by_id * sig)[d1].sum())
+        coef = np.where(d1, m_by_id * sig * (1 - sig) / width, 0.0)
+        coef[0] = 0.0
+        g = -(coef / np.where(r > 0, r, 1.0))[:, None] * d
+        g[0] -= g.sum(0)  # through the core's position
+        return Lv, g
+
+    def window(bodies):
+        be.upload(bodies)
+        be.compute_forces(p, False)
+        for _ in range(adj_steps):
+            be.kick(0.5 * dt)
+            be.drift(dt)
+            be.compute_forces(p, False)
+            be.kick(0.5 * dt)
+        ids = be.download().id
+        pos = np.zeros((n, 3))
+        pos[ids] = be.pos64().T
+        return pos
+
+    m_by_id = np.zeros(n)
+    m_by_id[bw.id] = bw.m
+    be.upload(bw)
+    be.synchronize()
+    be.event_record(12)
+    be.adjoint_forward(p, dt, adj_steps, every)
+    be.event_record(13)
+    ids = be.download().id
+    xT = np.zeros((n, 3))
+    xT[ids] = be.pos64().T
+    Lval, seed = loss_and_seed(xT, m_by_id)
+    be.event_record(14)
+    gx, gv, gm = be.adjoint_backward_seeded(seed)
+    be.event_record(15)
+    ck_ms = be.event_elapsed(12, 13) / adj_steps
+    adj_ms = be.event_elapsed(14, 15) / adj_steps
+    grad = f1 * gv[d1].sum(0) - f0 * gv[~d1].sum(0)
+    # The relative-velocity gradient is tiny over the window (both disks translate almost rigidly,
+    # the loss is measured about the disk-1 core), below what differences of FP32-force runs resolve.
+    # The check is therefore along the full velocity gradient: plain runs from the same window start
+    # with velocities moved by +-h gv/|gv| (lists rebuilt, not frozen), against |gv|.
+    gnorm = float(np.linalg.norm(gv))
+    u = gv / max(gnorm, 1e-300)
+    lp, lm_ = [], []
+    for sgn, out in ((1.0, lp), (-1.0, lm_)):
+        bb = bw.copy()
+        dv = sgn * h * u[bb.id]
+        bb.vx = (bb.vx + dv[:, 0]).astype(np.float32)
+        bb.vy = (bb.vy + dv[:, 1]).astype(np.float32)
+        bb.vz = (bb.vz + dv[:, 2]).astype(np.float32)
+        out.append(loss_and_seed(window(bb), m_by_id)[0])
+    fd = (lp[0] - lm_[0]) / (2 * h)
+    be.close()
+    return {"n": n, "n_each": ne, "steps": steps, "adjoint_steps": adj_steps, "checkpoint_every": every,
+            "generate_s": round(gen_s, 2), "forward_ms_per_step": round(fwd_ms, 3),
+            "checkpointed_forward_ms_per_step": round(ck_ms, 3), "adjoint_ms_per_step": round(adj_ms, 3),
+            "adjoint_over_forward": round(adj_ms / fwd_ms, 3),
+            "loss": Lval, "dL_dvrel": grad.tolist(), "dL_dvrel_norm": float(np.linalg.norm(grad)),
+            "velocity_gradient_norm": gnorm, "fd_along_velocity_gradient": fd,
+            "fd_rel_diff": float(abs(fd - gnorm) / max(abs(fd), 1e-300)), "fd_step": h,
+            "loss_radius": radius, "loss_width": width}
+
+
 def read_profile_traffic(workload):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -462,6 +567,10 @@ def run_gb300(args, w, world, rank, local, dist):
     if rank == 0 and not args.no_ensemble:
         ens = ensemble_leg(L, local, steps=args.ensemble_steps)
 
+    coll = None
+    if rank == 0 and args.collision:
+        coll = collision_leg(L, local, n_each=args.collision_n)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
@@ -483,6 +592,7 @@ def run_gb300(args, w, world, rank, local, dist):
             "cpu_baseline": cpu,
             "adjoint": adj,
             "ensemble": ens,
+            "collision": coll,
             "e2e": {"value": round(e2e_ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n},
             "gpu_launches": int(launches),
@@ -507,6 +617,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=1000, help="KDK steps of the adjoint leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--ensemble-steps", type=int, default=200, help="KDK steps of the ensemble leg")
+    ap.add_argument("--collision", action="store_true", help="run the two-disk collision leg (adjoint window)")
+    ap.add_argument("--collision-n", type=int, default=8_000_000, help="bodies per disk of the collision leg")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     world, rank, local, dist = dist_setup()

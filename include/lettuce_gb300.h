@@ -165,16 +165,26 @@ lg_status lg_host_free(void* p);
 
 /* ---- Adjoint of the leapfrog (no counterpart in the reference) -------------------------------
  * Reverse-mode derivative of the loss L = sum_i m_i |x_i(T) - x*_i|^2 after `steps` KDK steps of
- * size dt from the resident state, with direct-summation forces. lg_adjoint_forward runs the steps
- * (the final state stays resident, as after ordinary steps) and keeps FP64-position / FP32-velocity
- * checkpoints every `checkpoint_every` steps. lg_adjoint_backward takes x* (FP64, indexed by body
- * id; ids must be 0..n-1) and returns L and dL/dx0, dL/dv0, dL/dm (FP64, indexed by id); it
- * recomputes each segment from its checkpoint and applies one pairwise vector-Jacobian product per
- * step. Afterwards the resident state is no longer the final state (upload again to continue). */
+ * size dt from the resident state, with direct-summation or tree forces (p->method).
+ * lg_adjoint_forward runs the steps (the final state stays resident, as after ordinary steps) and
+ * keeps FP64-position / FP32-velocity checkpoints every `checkpoint_every` steps.
+ * lg_adjoint_backward takes x* (FP64, indexed by body id; ids must be 0..n-1) and returns L and
+ * dL/dx0, dL/dv0, dL/dm (FP64, indexed by id); it recomputes each segment from its checkpoint and
+ * applies one vector-Jacobian product per step: pairwise for direct forces; for tree forces over
+ * the step's interaction lists, held fixed ("frozen": the segment replay rebuilds the same tree
+ * from bit-identical positions), with the cell moments differentiated through the bodies.
+ * Afterwards the resident state is no longer the final state (upload again to continue). */
 lg_status lg_adjoint_forward(lg_engine* e, const lg_force_params* p, double dt, int steps, int checkpoint_every);
 lg_status lg_adjoint_backward(lg_engine* e, const double* target_x, const double* target_y, const double* target_z,
                               double* loss, double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz,
                               double* gm);
+/* Backward pass for any loss of the final positions: the caller passes dL/dx(T) (FP64, by body id;
+ * computed from the final state the forward pass left resident) and receives dL/dx0, dL/dv0 and
+ * the part of dL/dm that flows through the dynamics (an explicit dependence of L on the masses is
+ * the caller's to add). Losses that depend on the final velocities are not covered. */
+lg_status lg_adjoint_backward_seeded(lg_engine* e, const double* dldx, const double* dldy, const double* dldz,
+                                     double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz,
+                                     double* gm);
 
 /* ---- Batched ensembles (no reference counterpart) ----------------------------------------------
  * Many independent systems of uneven N advanced together: every force phase is one launch pipeline

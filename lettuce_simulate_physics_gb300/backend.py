@@ -178,6 +178,7 @@ def _lib() -> C.CDLL:
         "lg_host_alloc": (st, [C.c_size_t, C.POINTER(vp)]),
         "lg_adjoint_forward": (st, [vp, C.POINTER(_CForceParams), C.c_double, C.c_int, C.c_int]),
         "lg_adjoint_backward": (st, [vp, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d]),
+        "lg_adjoint_backward_seeded": (st, [vp, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d]),
         "lg_host_free": (st, [vp]),
         "lg_ensemble_create": (st, [C.c_int, C.POINTER(vp)]),
         "lg_ensemble_destroy": (st, [vp]),
@@ -428,6 +429,17 @@ class CudaBackend:
         _check(self._lib.lg_adjoint_backward(self._h, t[0].ctypes.data_as(_d), t[1].ctypes.data_as(_d),
                                              t[2].ctypes.data_as(_d), C.byref(loss), *ptr))
         return float(loss.value), out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
+
+    def adjoint_backward_seeded(self, dldx):
+        """Gradients for a caller's loss of the final positions: dldx (n, 3) = dL/dx(T) by body id.
+        Returns (gx (n,3), gv (n,3), gm (n,)) by id; gm excludes explicit mass dependence of L."""
+        n = self.size()
+        t = np.ascontiguousarray(np.asarray(dldx, np.float64).reshape(n, 3).T)
+        out = np.zeros((7, n), np.float64)
+        ptr = [out[k].ctypes.data_as(_d) for k in range(7)]
+        _check(self._lib.lg_adjoint_backward_seeded(self._h, t[0].ctypes.data_as(_d), t[1].ctypes.data_as(_d),
+                                                    t[2].ctypes.data_as(_d), *ptr))
+        return out[0:3].T.copy(), out[3:6].T.copy(), out[6].copy()
 
     def launch_count(self) -> int:
         c = C.c_uint64()

@@ -263,6 +263,21 @@ __global__ void k_tree_vjp_apply(const BodyArrays b, const double* g, int n, dou
     lm[k] += G * g[3 * static_cast<size_t>(n) + i];
 }
 
+// Terminal adjoints supplied by the caller (dL/dx_T by id): lx = seed, lv = 0, lm = 0. by_id selects
+// the tree path's id indexing; the direct path indexes by body position.
+__global__ void k_adj_seed(const BodyArrays b, const double* sx, const double* sy, const double* sz, double* lx,
+                           double* ly, double* lz, double* lvx, double* lvy, double* lvz, double* lm, double* loss_terms,
+                           int n, int by_id) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t id = b.id[i];
+    const uint32_t k = by_id ? id : static_cast<uint32_t>(i);
+    lx[k] = sx[id]; ly[k] = sy[id]; lz[k] = sz[id];
+    lvx[k] = lvy[k] = lvz[k] = 0;
+    lm[k] = 0;
+    loss_terms[k] = 0;
+}
+
 // Terminal adjoints indexed by id.
 __global__ void k_adj_init_id(const BodyArrays b, const double* tx, const double* ty, const double* tz, double* lx,
                               double* ly, double* lz, double* lvx, double* lvy, double* lvz, double* lm,
@@ -423,7 +438,7 @@ void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, doubl
 }
 
 double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const double* ty, const double* tz, double* gx,
-                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm) {
+                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm, bool seeded) {
     if (!a.have_forward || a.n != e.n) fail(kLogic, "adjoint backward: run the adjoint forward pass first");
     LG_CK(cudaSetDevice(e.dev));
     const int n = a.n;
@@ -450,7 +465,17 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     const int gb = grid_for(n, 256);
     // The forward pass left the final state resident: terminal adjoints from it (by body index for
     // the direct path, whose order never changes; by id for the tree path).
-    if (tree) {
+    if (seeded) {
+        k_adj_seed<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
+                                      a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                      a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(), a.loss_terms.as<double>(),
+                                      n, tree ? 1 : 0);
+        LG_LAUNCHED();
+        if (tree) {
+            k_mass_by_id<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.m_by_id.as<float>(), n);
+            LG_LAUNCHED();
+        }
+    } else if (tree) {
         k_adj_init_id<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.tx.as<double>(), a.ty.as<double>(), a.tz.as<double>(),
                                          a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
                                          a.lvy.as<double>(), a.lvz.as<double>(), a.lm.as<double>(),

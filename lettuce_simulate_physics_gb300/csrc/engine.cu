@@ -703,8 +703,20 @@ lg_status lg_adjoint_backward(lg_engine* e, const double* tx, const double* ty, 
         need(ty, "target_y");
         need(tz, "target_z");
         Engine& E = eng(e);
-        const double L = lg::adjoint_backward(E, *E.adjoint, tx, ty, tz, gx, gy, gz, gvx, gvy, gvz, gm);
+        const double L = lg::adjoint_backward(E, *E.adjoint, tx, ty, tz, gx, gy, gz, gvx, gvy, gvz, gm, false);
         if (loss) *loss = L;
+    });
+}
+
+lg_status lg_adjoint_backward_seeded(lg_engine* e, const double* dldx, const double* dldy, const double* dldz,
+                                     double* gx, double* gy, double* gz, double* gvx, double* gvy, double* gvz,
+                                     double* gm) {
+    return guard([&] {
+        need(dldx, "dldx");
+        need(dldy, "dldy");
+        need(dldz, "dldz");
+        Engine& E = eng(e);
+        lg::adjoint_backward(E, *E.adjoint, dldx, dldy, dldz, gx, gy, gz, gvx, gvy, gvz, gm, true);
     });
 }
 

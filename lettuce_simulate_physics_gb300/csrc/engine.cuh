@@ -154,8 +154,9 @@ void tree_walk_vjp(Engine& e, const float4* w, float e2, bool eps0, double* g);
 // adjoint.cu
 std::unique_ptr<AdjointState, void (*)(AdjointState*)> make_adjoint_state();
 void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, double dt, int steps, int every);
+// tx, ty, tz: the target x* (loss sum m |x_T - x*|^2), or with seeded the caller's dL/dx_T (by id).
 double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const double* ty, const double* tz, double* gx,
-                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm);
+                        double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm, bool seeded);
 // integrate.cu
 double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink);
 

@@ -174,3 +174,24 @@ def test_tree_adjoint_vs_frozen_list_central_differences(be, theta):
     print(f"theta={theta}: directional {ad:.9e} vs FD {fd:.9e}; worst sampled {worst:.2e}")
     assert abs(ad - fd) <= 1e-4 * abs(fd), (ad, fd)
     fz.close()
+
+
+@pytest.mark.parametrize("method", [L.ForceMethod.direct, L.ForceMethod.tree])
+def test_seeded_backward_equals_the_target_loss(be, method):
+    """lg_adjoint_backward_seeded with dL/dx(T) = 2 m (x(T) - x*) gives the target loss's gradients
+    (the mass gradient less the loss's explicit |x(T) - x*|^2)."""
+    b = S.plummer(500, 8, cut=10)
+    p = L.ForceParams(G=1.0, eps=0.03, theta=0.5, method=method)
+    dt, steps, every = 1e-3, 10, 4
+    be.upload(b)
+    be.adjoint_forward(p, dt, steps, every)
+    xT = _by_id(be, be.pos64())
+    rng = np.random.Generator(np.random.PCG64(9))
+    xstar = xT + rng.normal(0, 1e-2, xT.shape)
+    m = b.m.astype(np.float64)
+    gx1, gv1, gm1 = be.adjoint_backward_seeded(2 * m[:, None] * (xT - xstar))
+    be.upload(b)
+    be.adjoint_forward(p, dt, steps, every)
+    _, gx2, gv2, gm2 = be.adjoint_backward(xstar)
+    assert np.array_equal(gx1, gx2) and np.array_equal(gv1, gv2)
+    np.testing.assert_allclose(gm1 + ((xT - xstar) ** 2).sum(1), gm2, rtol=1e-12, atol=1e-14 * np.abs(gm2).max())
