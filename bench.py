@@ -195,10 +195,22 @@ def adjoint_leg(L, local, steps=1000, every=32, n=65536):
     loss, gx, gv, gm = be.adjoint_backward(xstar)
     be.event_record(7)
     adj_ms = be.event_elapsed(6, 7) / steps
+    # The same with a checkpoint at every step: every position kept (steps x N x 44 B, 2.9 GB here),
+    # so the backward pass needs no recomputation.
+    be.upload(b)
+    be.adjoint_forward(p, dt, steps, 1)
+    be.synchronize()
+    be.event_record(6)
+    loss1, gx1, _, _ = be.adjoint_backward(xstar)
+    be.event_record(7)
+    adj1_ms = be.event_elapsed(6, 7) / steps
     be.close()
     return {"n": n, "steps": steps, "checkpoint_every": every, "loss": loss,
             "forward_ms_per_step": round(fwd_ms, 4), "checkpointed_forward_ms_per_step": round(ck_fwd_ms, 4),
             "adjoint_ms_per_step": round(adj_ms, 4), "adjoint_over_forward": round(adj_ms / fwd_ms, 3),
+            "every_step_checkpoints": {"adjoint_ms_per_step": round(adj1_ms, 4),
+                                       "adjoint_over_forward": round(adj1_ms / fwd_ms, 3),
+                                       "same_gradient": bool(np.array_equal(gx, gx1))},
             "grad_norms": {"x": float(np.linalg.norm(gx)), "v": float(np.linalg.norm(gv)),
                            "m": float(np.linalg.norm(gm))}}
 

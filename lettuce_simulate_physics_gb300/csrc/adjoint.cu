@@ -1,4 +1,4 @@
-// Adjoint (reverse mode) of the kick-drift-kick leapfrog with direct-summation forces. The
+// Adjoint (reverse mode) of the kick-drift-kick leapfrog with direct-summation or tree forces. The
 // reference has no adjoint; this is the engine's own, checked against FP64 central finite
 // differences and the FP64 CPU adjoint in oracle/lettuce_oracle.c.
 //
@@ -39,9 +39,24 @@ namespace lg {
 
 namespace {
 
-constexpr int VBS = 256;
-constexpr int VTILE = 256;
-constexpr int VIPT = 2;
+// Launch shape of the pairwise VJP (measured best on GB300: 128 threads, one i-body per thread,
+// four j-pairs unrolled).
+#ifndef LG_VJP_BS
+#define LG_VJP_BS 128
+#endif
+#ifndef LG_VJP_IPT
+#define LG_VJP_IPT 1
+#endif
+#ifndef LG_VJP_UNROLL
+#define LG_VJP_UNROLL 4
+#endif
+#ifndef LG_VJP_MINB
+#define LG_VJP_MINB 1
+#endif
+constexpr int VBS = LG_VJP_BS;  // threads per block
+constexpr int VTILE = 256;      // j-bodies per shared-memory tile
+constexpr int VIPT = LG_VJP_IPT; // i-bodies per thread
+constexpr int VUNROLL = LG_VJP_UNROLL;  // j-pair iterations unrolled
 
 struct __align__(16) VjpSmem {
     float rx[VTILE], ry[VTILE], rz[VTILE], rm[VTILE], wx[VTILE], wy[VTILE], wz[VTILE];
@@ -52,8 +67,15 @@ inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) 
 __device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
 
 // partial[slice][i] = (gx, gy, gz, h) for the i-bodies of this block and the j of this slice.
+//
+// Factored pair sum. With c_j = (m_k (w_j . d) - m_j (w_k . d)) / s^5,
+//   sum_j M(d)(m_k w_j - m_j w_k) = m_k S1 - w_k S2 - 3 S3,
+//   S1 = sum_j w_j / s^3,  S2 = sum_j m_j / s^3,  S3 = sum_j c_j d,
+// so a pair costs 26 FP32 operations (packed two pairs at a time) instead of forming
+// m_k w_j - m_j w_k per pair. The self pair (d = 0) adds w_k / eps^3 to S1 and m_k / eps^3 to S2,
+// which are taken out again, exactly as the loop formed them, in the slice that holds it.
 template <bool EPS0>
-__global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, const float4* __restrict__ lo,
+__global__ void __launch_bounds__(VBS, LG_VJP_MINB) k_vjp(const float4* __restrict__ hm, const float4* __restrict__ lo,
                                              const float4* __restrict__ wv, int n, int jslice, float e2,
                                              float4* __restrict__ partial) {
     __shared__ VjpSmem sm;
@@ -62,28 +84,24 @@ __global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, cons
     const int j0 = blockIdx.y * jslice;
     const int j1 = min(n, j0 + jslice);
     const float4 oh = hm[base], ol = lo[base];
-    float xi[VIPT], yi[VIPT], zi[VIPT], mk[VIPT], wkx[VIPT], wky[VIPT], wkz[VIPT];
-    float s[VIPT][4], c[VIPT][4];
+    float mk[VIPT], wkx[VIPT], wky[VIPT], wkz[VIPT];
+    float s[VIPT][8], c[VIPT][8];  // S1 (3), S2 (negated), S3 (3), h: Kahan sums and compensations
+    f2x XI[VIPT], YI[VIPT], ZI[VIPT], MK[VIPT], WKX[VIPT], WKY[VIPT], WKZ[VIPT];
 #pragma unroll
     for (int u = 0; u < VIPT; ++u) {
         const int i = min(base + u * VBS + tid, n - 1);
         const float4 h = hm[i], l = lo[i], w = wv[i];
-        xi[u] = (h.x - oh.x) + (l.x - ol.x);
-        yi[u] = (h.y - oh.y) + (l.y - ol.y);
-        zi[u] = (h.z - oh.z) + (l.z - ol.z);
+        XI[u] = f2_bcast((h.x - oh.x) + (l.x - ol.x));
+        YI[u] = f2_bcast((h.y - oh.y) + (l.y - ol.y));
+        ZI[u] = f2_bcast((h.z - oh.z) + (l.z - ol.z));
         mk[u] = h.w;
         wkx[u] = w.x; wky[u] = w.y; wkz[u] = w.z;
+        MK[u] = f2_bcast(h.w);
+        WKX[u] = f2_bcast(w.x); WKY[u] = f2_bcast(w.y); WKZ[u] = f2_bcast(w.z);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) s[u][q] = c[u][q] = 0.f;
+        for (int q = 0; q < 8; ++q) s[u][q] = c[u][q] = 0.f;
     }
-    f2x XI[VIPT], YI[VIPT], ZI[VIPT], MK[VIPT], WKX[VIPT], WKY[VIPT], WKZ[VIPT];
-#pragma unroll
-    for (int u = 0; u < VIPT; ++u) {
-        XI[u] = f2_bcast(xi[u]); YI[u] = f2_bcast(yi[u]); ZI[u] = f2_bcast(zi[u]);
-        MK[u] = f2_bcast(mk[u]);
-        WKX[u] = f2_bcast(wkx[u]); WKY[u] = f2_bcast(wky[u]); WKZ[u] = f2_bcast(wkz[u]);
-    }
-    const f2x E2 = f2_bcast(e2), C3 = f2_bcast(3.f);
+    const f2x E2 = f2_bcast(e2);
     for (int jt = j0; jt < j1; jt += VTILE) {
         const int cnt = min(VTILE, j1 - jt);
         const int cnt2 = (cnt + 1) & ~1;
@@ -94,7 +112,7 @@ __global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, cons
                 sm.rx[k] = (h.x - oh.x) + (l.x - ol.x);
                 sm.ry[k] = (h.y - oh.y) + (l.y - ol.y);
                 sm.rz[k] = (h.z - oh.z) + (l.z - ol.z);
-                sm.rm[k] = h.w;
+                sm.rm[k] = -h.w;  // negated mass
                 sm.wx[k] = w.x; sm.wy[k] = w.y; sm.wz[k] = w.z;
             } else {
                 sm.rx[k] = sm.ry[k] = sm.rz[k] = 1e18f;  // far, massless, zero weight: adds nothing
@@ -103,12 +121,14 @@ __global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, cons
             }
         }
         __syncthreads();
-        f2x gx[VIPT], gy[VIPT], gz[VIPT], hh[VIPT];
+        f2x a[VIPT][8];
 #pragma unroll
-        for (int u = 0; u < VIPT; ++u) gx[u] = gy[u] = gz[u] = hh[u] = 0ull;
-#pragma unroll 1
+        for (int u = 0; u < VIPT; ++u)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) a[u][q] = 0ull;
+#pragma unroll VUNROLL
         for (int k = 0; k < cnt2; k += 2) {
-            const f2x X = ld2(sm.rx + k), Y = ld2(sm.ry + k), Z = ld2(sm.rz + k), M = ld2(sm.rm + k);
+            const f2x X = ld2(sm.rx + k), Y = ld2(sm.ry + k), Z = ld2(sm.rz + k), NM = ld2(sm.rm + k);
             const f2x WX = ld2(sm.wx + k), WY = ld2(sm.wy + k), WZ = ld2(sm.wz + k);
 #pragma unroll
             for (int u = 0; u < VIPT; ++u) {
@@ -123,33 +143,48 @@ __global__ void __launch_bounds__(VBS) k_vjp(const float4* __restrict__ hm, cons
                 }
                 const f2x inv = f2_pack(ia, ib);
                 const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv2, inv), inv5 = f2_mul(inv3, inv2);
-                // u = m_k w_j - m_j w_k
-                const f2x ux = f2_sub(f2_mul(MK[u], WX), f2_mul(M, WKX[u]));
-                const f2x uy = f2_sub(f2_mul(MK[u], WY), f2_mul(M, WKY[u]));
-                const f2x uz = f2_sub(f2_mul(MK[u], WZ), f2_mul(M, WKZ[u]));
-                const f2x du = f2_fma(dx, ux, f2_fma(dy, uy, f2_mul(dz, uz)));
-                const f2x t = f2_mul(f2_mul(C3, du), inv5);
-                gx[u] = f2_sub(f2_fma(ux, inv3, gx[u]), f2_mul(dx, t));
-                gy[u] = f2_sub(f2_fma(uy, inv3, gy[u]), f2_mul(dy, t));
-                gz[u] = f2_sub(f2_fma(uz, inv3, gz[u]), f2_mul(dz, t));
-                const f2x wd = f2_fma(WX, dx, f2_fma(WY, dy, f2_mul(WZ, dz)));
-                hh[u] = f2_fma(wd, inv3, hh[u]);
+                const f2x dwj = f2_fma(dx, WX, f2_fma(dy, WY, f2_mul(dz, WZ)));
+                const f2x dwk = f2_fma(dx, WKX[u], f2_fma(dy, WKY[u], f2_mul(dz, WKZ[u])));
+                const f2x cc = f2_mul(f2_fma(MK[u], dwj, f2_mul(NM, dwk)), inv5);
+                a[u][0] = f2_fma(WX, inv3, a[u][0]);
+                a[u][1] = f2_fma(WY, inv3, a[u][1]);
+                a[u][2] = f2_fma(WZ, inv3, a[u][2]);
+                a[u][3] = f2_fma(NM, inv3, a[u][3]);
+                a[u][4] = f2_fma(cc, dx, a[u][4]);
+                a[u][5] = f2_fma(cc, dy, a[u][5]);
+                a[u][6] = f2_fma(cc, dz, a[u][6]);
+                a[u][7] = f2_fma(dwj, inv3, a[u][7]);
             }
         }
 #pragma unroll
-        for (int u = 0; u < VIPT; ++u) {
-            kahan_add(s[u][0], c[u][0], f2_sum(gx[u]));
-            kahan_add(s[u][1], c[u][1], f2_sum(gy[u]));
-            kahan_add(s[u][2], c[u][2], f2_sum(gz[u]));
-            kahan_add(s[u][3], c[u][3], f2_sum(hh[u]));
-        }
+        for (int u = 0; u < VIPT; ++u)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) kahan_add(s[u][q], c[u][q], f2_sum(a[u][q]));
+    }
+    // The self pair's S1 and S2 terms, formed as the loop formed them (r2 == e2).
+    float self3 = 0.f;
+    if (!EPS0) {
+        const float inv = rsqrt_mufu(e2), inv2 = inv * inv;
+        self3 = inv2 * inv;
     }
 #pragma unroll
     for (int u = 0; u < VIPT; ++u) {
         const int i = base + u * VBS + tid;
         if (i >= n) continue;
-        partial[static_cast<size_t>(blockIdx.y) * n + i] =
-            make_float4(s[u][0] - c[u][0], s[u][1] - c[u][1], s[u][2] - c[u][2], s[u][3] - c[u][3]);
+        float S[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) S[q] = s[u][q] - c[u][q];
+        if (!EPS0 && i >= j0 && i < j1) {
+            S[0] = __fsub_rn(S[0], __fmul_rn(wkx[u], self3));
+            S[1] = __fsub_rn(S[1], __fmul_rn(wky[u], self3));
+            S[2] = __fsub_rn(S[2], __fmul_rn(wkz[u], self3));
+            S[3] = __fadd_rn(S[3], __fmul_rn(mk[u], self3));
+        }
+        // m_k S1 - w_k S2 - 3 S3 (S[3] holds -S2)
+        const float gx = mk[u] * S[0] + wkx[u] * S[3] - 3.f * S[4];
+        const float gy = mk[u] * S[1] + wky[u] * S[3] - 3.f * S[5];
+        const float gz = mk[u] * S[2] + wkz[u] * S[3] - 3.f * S[6];
+        partial[static_cast<size_t>(blockIdx.y) * n + i] = make_float4(gx, gy, gz, S[7]);
     }
 }
 
@@ -494,7 +529,15 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     LG_CK(cudaMemcpyAsync(terms.data(), a.loss_terms.as<double>(), nb8, cudaMemcpyDeviceToHost, s));
     // Direct VJP launch shape: whole waves over split-j slices.
     const int iblocks = (n + VBS * VIPT - 1) / (VBS * VIPT);
-    int slices = std::max(1, std::min(n / 128 + 1, (2 * e.sms + iblocks - 1) / iblocks));
+    static int vjp_per_sm = 0;
+    if (!vjp_per_sm) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&vjp_per_sm, k_vjp<false>, VBS, 0) != cudaSuccess) {
+            cudaGetLastError();
+            vjp_per_sm = 2;
+        }
+        if (vjp_per_sm < 1) vjp_per_sm = 1;
+    }
+    int slices = std::max(1, std::min(n / 128 + 1, (vjp_per_sm * e.sms + iblocks - 1) / iblocks));
     int jslice = (n + slices - 1) / slices;
     slices = (n + jslice - 1) / jslice;
     if (!tree) a.partial.reserve(static_cast<size_t>(slices) * n * 16);
@@ -504,20 +547,36 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     for (int seg = (a.steps - 1) / a.every; seg >= 0; --seg) {
         const int s0 = seg * a.every, s1 = std::min(a.steps, s0 + a.every);
         // Restore the checkpoint at s0 and recompute the segment's positions.
+        // Only positions are needed: the forces at the segment's last position (and the closing
+        // kick after them) are skipped, so a segment of k steps costs k - 1 force evaluations.
         restore_ck(e, a, seg);
+        const bool more = s1 - s0 >= 2;
         if (tree) {
-            tree_forces(e, a.p);
+            if (more) tree_forces(e, a.p);
             store_step(e, a, 0);
             for (int st = s0; st < s1 - 1; ++st) {
-                kdk_step_tree(e, a.p, a.dt);
+                e.kick(0.5 * a.dt);
+                e.drift(a.dt);
+                if (st + 1 < s1 - 1) {
+                    tree_forces(e, a.p);
+                    e.kick(0.5 * a.dt);
+                }
+                // Unsorted at the last step: the VJP's rebuild sorts it as the forward pass did.
                 store_step(e, a, st - s0 + 1);
             }
         } else {
-            direct_forces(e, a.p);
+            if (more) direct_forces(e, a.p);
             k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>(), a.seg_lo.as<float4>(), n);
             LG_LAUNCHED();
             for (int st = s0; st < s1 - 1; ++st) {
-                kdk_step(e, a.p, a.dt);
+                launch_kick(e.bodies(e.cur), e.acc.as<float4>(), static_cast<float>(0.5 * a.dt), n, s);
+                launch_drift(e.bodies(e.cur), a.dt, n, s);
+                e.launches += 2;
+                if (st + 1 < s1 - 1) {
+                    direct_forces(e, a.p);
+                    launch_kick(e.bodies(e.cur), e.acc.as<float4>(), static_cast<float>(0.5 * a.dt), n, s);
+                    ++e.launches;
+                }
                 const size_t so = static_cast<size_t>(st - s0 + 1) * n;
                 k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
                                                n);

@@ -24,6 +24,13 @@ namespace lg {
 
 namespace {
 
+#ifndef LG_DIRECT_UNROLL
+#define LG_DIRECT_UNROLL 2  // j-pair iterations unrolled in the inner loop (measured best on GB300)
+#endif
+#ifndef LG_DIRECT_MINB
+#define LG_DIRECT_MINB 1    // resident blocks per SM the register budget is sized for
+#endif
+constexpr int DUNROLL = LG_DIRECT_UNROLL;
 constexpr int DBS = 256;   // threads per block
 constexpr int TILE = 256;  // j-bodies per stage
 
@@ -132,7 +139,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
         const float* ry = sm.ry[buf];
         const float* rz = sm.rz[buf];
         const float* rm = sm.rm[buf];
-#pragma unroll 1
+#pragma unroll DUNROLL
         for (int k = 0; k < cnt8; k += 2) {
             const f2x X = *reinterpret_cast<const f2x*>(rx + k), Y = *reinterpret_cast<const f2x*>(ry + k);
             const f2x Z = *reinterpret_cast<const f2x*>(rz + k), M = *reinterpret_cast<const f2x*>(rm + k);
@@ -189,7 +196,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
 }
 
 template <int IPT, bool POT, bool EPS0>
-__global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
+__global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
                                                 int jslice, float G, float e2, float4* __restrict__ out, int write_final,
                                                 unsigned* err) {
     __shared__ DirectSmem sm;
@@ -201,7 +208,7 @@ __global__ void __launch_bounds__(DBS) k_direct(const float4* __restrict__ hm, c
 // Many independent systems in one launch: block b takes work item b (an i-tile of one system
 // against all of that system's bodies), with the system's own softening.
 template <int IPT, bool POT, bool EPS0>
-__global__ void __launch_bounds__(DBS) k_direct_batch(const float4* __restrict__ hm, const float4* __restrict__ lo,
+__global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct_batch(const float4* __restrict__ hm, const float4* __restrict__ lo,
                                                       const DirectWork* __restrict__ work, float G,
                                                       float4* __restrict__ acc, unsigned* err) {
     __shared__ DirectSmem sm;
@@ -238,6 +245,29 @@ void launch_ipt(const BodyArrays b, int n, float G, float e2, bool pot, bool eps
     LG_LAUNCHED();
 }
 
+// Resident blocks per SM of the i-bodies-per-thread variant (no potential), from the occupancy
+// calculator; cached per variant.
+int blocks_per_sm(int ipt) {
+    static int cache[9] = {};
+    const int k = ipt == 1 ? 1 : (ipt == 2 ? 2 : (ipt == 8 ? 8 : 4));
+    if (!cache[k]) {
+        int per = 0;
+        cudaError_t e = cudaSuccess;
+        switch (k) {
+            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<1, false, false>, DBS, 0); break;
+            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<2, false, false>, DBS, 0); break;
+            case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<8, false, false>, DBS, 0); break;
+            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<4, false, false>, DBS, 0); break;
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            per = 2;
+        }
+        cache[k] = per < 1 ? 1 : per;
+    }
+    return cache[k];
+}
+
 }  // namespace
 
 // Default shape: i-bodies per thread by size, and a split-j count that makes the grid a whole
@@ -247,7 +277,7 @@ DirectShape default_direct_shape(int n, int sms) {
     sh.ipt = n >= 8 * 1024 ? 4 : (n >= 2048 ? 2 : 1);
     sh.tile = TILE;
     const int iblocks = (n + DBS * sh.ipt - 1) / (DBS * sh.ipt);
-    const int wave = 2 * sms;  // two 256-thread blocks of the IPT-4 kernel fit per SM
+    const int wave = blocks_per_sm(sh.ipt) * sms;
     const int max_slices = std::max(1, n / 128);
     int best = 1;
     double best_eff = 0;

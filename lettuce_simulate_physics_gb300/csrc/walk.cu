@@ -31,6 +31,14 @@ constexpr int WBS = 128;  // 4 warps per block
 #ifndef LG_WALK_MINB
 #define LG_WALK_MINB 4  // resident blocks per SM the register budget is sized for
 #endif
+#ifndef LG_WALK_CUNROLL
+#define LG_WALK_CUNROLL 1  // cell-entry pairs unrolled in the evaluation loop
+#endif
+#ifndef LG_WALK_BUNROLL
+#define LG_WALK_BUNROLL 2  // body-entry pairs unrolled in the evaluation loop
+#endif
+constexpr int CUNROLL = LG_WALK_CUNROLL;
+constexpr int BUNROLL = LG_WALK_BUNROLL;
 constexpr int WARPS = WBS / 32;
 constexpr int CCH = 64;   // cells converted per chunk
 constexpr int BCH = 128;  // bodies converted per chunk
@@ -110,7 +118,7 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int lane, const 
     }
     const f2x E2 = f2_bcast(e2), C25 = f2_bcast(2.5f), NEG1 = f2_bcast(-1.f), C05 = f2_bcast(0.5f);
     // Few i-bodies per lane leave little independent work per entry: unroll over entries then.
-#pragma unroll 1
+#pragma unroll CUNROLL
     for (int k = 0; k < cc; k += 2) {
         const f2x X = ld2(s.cx + k), Y = ld2(s.cy + k), Z = ld2(s.cz + k), M = ld2(s.cm + k);
         const f2x QXX = ld2(s.qxx + k), QXY = ld2(s.qxy + k), QXZ = ld2(s.qxz + k);
@@ -151,7 +159,7 @@ __device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int lane, const
         ax[u] = ay[u] = az[u] = ap[u] = 0ull;
     }
     const f2x E2 = f2_bcast(e2);
-#pragma unroll 2
+#pragma unroll BUNROLL
     for (int k = 0; k < bc; k += 2) {
         const f2x X = ld2(s.bx + k), Y = ld2(s.by + k), Z = ld2(s.bz + k), M = ld2(s.bm + k);
 #pragma unroll
