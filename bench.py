@@ -529,8 +529,14 @@ def run_gb300(args, w, world, rank, local, dist):
             cells.append(ct)
         be.synchronize()
         wall = time.perf_counter() - t0
+        launches = be.launch_count() - launches0
+        # The same step under load for a few hundred milliseconds more, so that the 200 ms clock
+        # samples cover the step (not timed).
+        t1 = time.perf_counter()
+        while time.perf_counter() - t1 < 0.6:
+            step()
+            be.synchronize()
     barrier(dist)
-    launches = be.launch_count() - launches0
     ms = reduce_max(dist, statistics.fmean(step_ms))
     clocks = clk.summary()
 
@@ -573,15 +579,16 @@ def run_gb300(args, w, world, rank, local, dist):
 
     adj = None
     if rank == 0 and not args.no_adjoint:
-        adj = adjoint_leg(L, local, steps=args.adjoint_steps)
+        adj = adjoint_leg(L, local, steps=args.adjoint_steps, n=args.adjoint_n)
 
     ens = None
     if rank == 0 and not args.no_ensemble:
-        ens = ensemble_leg(L, local, steps=args.ensemble_steps)
+        ens = ensemble_leg(L, local, steps=args.ensemble_steps, count=args.ensemble_count)
 
     coll = None
     if rank == 0 and args.collision:
-        coll = collision_leg(L, local, n_each=args.collision_n)
+        coll = collision_leg(L, local, n_each=args.collision_n, steps=args.collision_steps,
+                             adj_steps=args.collision_adj_steps, every=args.collision_every)
 
     if rank == 0:
         line = {
@@ -631,8 +638,28 @@ def main():
     ap.add_argument("--ensemble-steps", type=int, default=200, help="KDK steps of the ensemble leg")
     ap.add_argument("--collision", action="store_true", help="run the two-disk collision leg (adjoint window)")
     ap.add_argument("--collision-n", type=int, default=8_000_000, help="bodies per disk of the collision leg")
+    ap.add_argument("--collision-steps", type=int, default=500, help="KDK steps of the collision leg")
+    ap.add_argument("--collision-adj-steps", type=int, default=64, help="adjoint window of the collision leg")
+    ap.add_argument("--collision-every", type=int, default=8, help="checkpoint interval of the collision window")
+    ap.add_argument("--adjoint-n", type=int, default=65536, help="bodies of the adjoint leg")
+    ap.add_argument("--ensemble-count", type=int, default=512, help="systems of the ensemble leg")
+    ap.add_argument("--only", choices=["adjoint", "ensemble", "collision"],
+                    help="run one leg alone (single GPU) and print its JSON result")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
+    if args.only:
+        import lettuce_simulate_physics_gb300 as L
+        from lettuce_simulate_physics_gb300 import build as B
+        B.build()
+        if args.only == "adjoint":
+            out = adjoint_leg(L, 0, steps=args.adjoint_steps, n=args.adjoint_n)
+        elif args.only == "ensemble":
+            out = ensemble_leg(L, 0, steps=args.ensemble_steps, count=args.ensemble_count)
+        else:
+            out = collision_leg(L, 0, n_each=args.collision_n, steps=args.collision_steps,
+                                adj_steps=args.collision_adj_steps, every=args.collision_every)
+        print(json.dumps({"leg": args.only, **out}), flush=True)
+        return 0
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
         return run_reference(args, w, world, rank, dist)
