@@ -114,10 +114,41 @@ lg_status lg_local_bounds(lg_engine* e, float lo[3], float hi[3]);
 /* Backend::build_tree(p), src/backend.hpp:118: sort and build for the current positions;
  * invalidates accelerations, potential and costs; no-op for the direct method. */
 lg_status lg_build_tree(lg_engine* e, const lg_force_params* p);
-/* Backend::compute_forces_with(p, potential, remote), src/backend.hpp:128-129, with an empty
- * remote list (the MPI locally-essential-tree exchange is not part of this engine; nremote > 0
- * returns LG_ERR_RUNTIME). LG_ERR_LOGIC for the tree method without a current tree. */
-lg_status lg_compute_forces_with(lg_engine* e, const lg_force_params* p, int potential, size_t nremote);
+/* LetNode, src/backend.hpp:62-75: the same 60-byte layout, so a LetTree's node array can be passed
+ * as is. Receiver rule (src/backend.hpp:77-82): a node with no children and no bodies, or with
+ * |box distance|^2 >= rcrit2, is a multipole; otherwise its bodies, or else its children. */
+typedef struct {
+    float cx, cy, cz;
+    float mass;
+    float qxx, qxy, qxz, qyy, qyz, qzz;
+    float rcrit2;
+    int32_t first_child, child_count;
+    int32_t body_first, body_count;
+} lg_let_node;
+
+/* LetTree, src/backend.hpp:83-86: nodes (root first) and its bodies. */
+typedef struct {
+    const lg_let_node* nodes;
+    size_t nnodes;
+    const float *bx, *by, *bz, *bm;
+    size_t nbodies;
+} lg_let_tree;
+
+/* Backend::compute_forces_with(p, potential, remote), src/backend.hpp:128-129: forces from the
+ * resident bodies' own tree (or direct sum) plus the `nremote` locally-essential trees of other
+ * ranks, walked on the device with the receiver rule (tree method: per walk group; direct method:
+ * per block of 128 consecutive bodies, as src/cpu_backend.cpp:695-717). LG_ERR_LOGIC for the tree
+ * method without a current tree. */
+lg_status lg_compute_forces_with(lg_engine* e, const lg_force_params* p, int potential, const lg_let_tree* remote,
+                                 size_t nremote);
+/* Backend::export_let(target, p), src/backend.hpp:120-124: the part of this engine's tree that any
+ * target inside the box lo..hi could open, built on the device in the reference's breadth-first
+ * order (src/cpu_backend.cpp:222-270); the direct method exports one always-open root holding every
+ * body. lg_export_let builds it and returns its sizes; lg_export_let_read copies it out (arrays of
+ * the sizes returned). LG_ERR_LOGIC for the tree method without a current tree. */
+lg_status lg_export_let(lg_engine* e, const float lo[3], const float hi[3], const lg_force_params* p, size_t* nnodes,
+                        size_t* nbodies);
+lg_status lg_export_let_read(lg_engine* e, lg_let_node* nodes, float* bx, float* by, float* bz, float* bm);
 /* Backend::memory_need(n, method), src/backend.hpp:131. */
 lg_status lg_memory_need(uint64_t n, int method, lg_memory_estimate* out);
 /* Backend::device_memory(free, total), src/backend.hpp:134-137; free includes what the engine holds. */

@@ -6,6 +6,6 @@ holds the seeded workloads; ``build`` compiles the library in-tree with nvcc.
 """
 from .bodies import Bodies  # noqa: F401
 from .backend import (  # noqa: F401
-    Box3, CudaBackend, Diag, ForceMethod, ForceParams, LogicError, MemoryNeed, PhaseTimes, UnavailableError,
+    Box3, CudaBackend, Diag, ForceMethod, ForceParams, LetTree, LogicError, MemoryNeed, PhaseTimes, UnavailableError,
     cuda_compiled, cuda_device_count, library_path, make_cuda_backend,
 )

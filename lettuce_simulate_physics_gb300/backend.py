@@ -120,6 +120,30 @@ class _CEnsTuning(C.Structure):
     _fields_ = [("direct_ipt", C.c_int * 3), ("walk_group", C.c_int), ("tuned", C.c_int)]
 
 
+# LetNode (src/backend.hpp:62-75): the 60-byte record of a locally-essential tree node.
+LET_NODE_DTYPE = np.dtype([("cx", "<f4"), ("cy", "<f4"), ("cz", "<f4"), ("mass", "<f4"), ("qxx", "<f4"),
+                           ("qxy", "<f4"), ("qxz", "<f4"), ("qyy", "<f4"), ("qyz", "<f4"), ("qzz", "<f4"),
+                           ("rcrit2", "<f4"), ("first_child", "<i4"), ("child_count", "<i4"),
+                           ("body_first", "<i4"), ("body_count", "<i4")])
+assert LET_NODE_DTYPE.itemsize == 60
+
+
+@dataclass
+class LetTree:
+    """LetTree (src/backend.hpp:83-86): nodes (root first) and their bodies."""
+    nodes: np.ndarray = field(default_factory=lambda: np.zeros(0, LET_NODE_DTYPE))
+    bx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    by: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    bz: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    bm: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+
+
+class _CLetTree(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("nnodes", C.c_size_t), ("bx", C.POINTER(C.c_float)),
+                ("by", C.POINTER(C.c_float)), ("bz", C.POINTER(C.c_float)), ("bm", C.POINTER(C.c_float)),
+                ("nbodies", C.c_size_t)]
+
+
 _f = C.POINTER(C.c_float)
 _u = C.POINTER(C.c_uint32)
 _d = C.POINTER(C.c_double)
@@ -157,7 +181,9 @@ def _lib() -> C.CDLL:
         "lg_times": (st, [vp, C.POINTER(_CTimes)]),
         "lg_local_bounds": (st, [vp, _f, _f]),
         "lg_build_tree": (st, [vp, C.POINTER(_CForceParams)]),
-        "lg_compute_forces_with": (st, [vp, C.POINTER(_CForceParams), C.c_int, C.c_size_t]),
+        "lg_compute_forces_with": (st, [vp, C.POINTER(_CForceParams), C.c_int, C.POINTER(_CLetTree), C.c_size_t]),
+        "lg_export_let": (st, [vp, _f, _f, C.POINTER(_CForceParams), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+        "lg_export_let_read": (st, [vp, C.c_void_p, _f, _f, _f, _f]),
         "lg_memory_need": (st, [C.c_uint64, C.c_int, C.POINTER(_CMem)]),
         "lg_device_memory": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "lg_body_costs": (st, [vp, _f, C.c_size_t, C.POINTER(C.c_int)]),
@@ -323,8 +349,31 @@ class CudaBackend:
         _check(self._lib.lg_build_tree(self._h, C.byref(cp)))
 
     def compute_forces_with(self, p: ForceParams, potential: bool = False, remote=()) -> None:
+        """Forces from the own tree (or direct sum) plus other ranks' locally-essential trees."""
         cp = _cparams(p)
-        _check(self._lib.lg_compute_forces_with(self._h, C.byref(cp), int(bool(potential)), len(remote)))
+        keep = []
+        arr = (_CLetTree * max(len(remote), 1))()
+        for k, t in enumerate(remote):
+            if not isinstance(t, LetTree):
+                raise TypeError("remote entries must be LetTree")
+            nodes = np.ascontiguousarray(t.nodes, LET_NODE_DTYPE)
+            cols = [np.ascontiguousarray(getattr(t, c), np.float32) for c in ("bx", "by", "bz", "bm")]
+            keep += [nodes, *cols]
+            arr[k] = _CLetTree(nodes.ctypes.data if len(nodes) else None, len(nodes), *(_fp(c) for c in cols),
+                               len(cols[0]))
+        _check(self._lib.lg_compute_forces_with(self._h, C.byref(cp), int(bool(potential)), arr, len(remote)))
+
+    def export_let(self, lo, hi, p: ForceParams) -> LetTree:
+        """The part of this engine's tree any target in the box lo..hi could open."""
+        cp = _cparams(p)
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        nn, nb = C.c_size_t(), C.c_size_t()
+        _check(self._lib.lg_export_let(self._h, _fp(lo), _fp(hi), C.byref(cp), C.byref(nn), C.byref(nb)))
+        t = LetTree(np.zeros(nn.value, LET_NODE_DTYPE), *(np.zeros(nb.value, np.float32) for _ in range(4)))
+        _check(self._lib.lg_export_let_read(self._h, t.nodes.ctypes.data if nn.value else None, _fp(t.bx),
+                                            _fp(t.by), _fp(t.bz), _fp(t.bm)))
+        return t
 
     @staticmethod
     def memory_need(n: int, method: ForceMethod) -> MemoryNeed:

@@ -53,6 +53,10 @@ class Bodies:
         return cls(pos[:, 0], pos[:, 1], pos[:, 2], vel[:, 0], vel[:, 1], vel[:, 2],
                    np.broadcast_to(np.asarray(m, np.float64), (n,)), ids)
 
+    def subset(self, sel) -> "Bodies":
+        """The bodies a boolean mask or index array selects, ids kept."""
+        return Bodies(*(getattr(self, f)[sel] for f in _FIELDS), self.id[sel])
+
     def copy(self) -> "Bodies":
         return Bodies(*(getattr(self, f).copy() for f in _FIELDS + ("id",)))
 

@@ -386,7 +386,7 @@ void restore_ck(Engine& e, AdjointState& a, int slot) {
 // Tree forces through the engine's own build and walk (sizes checked, as every force call).
 void tree_forces(Engine& e, const lg_force_params& p) {
     e.build_tree(p);
-    e.compute_forces_with(p, false, 0);
+    e.compute_forces_with(p, false, nullptr, 0);
 }
 
 void kdk_step_tree(Engine& e, const lg_force_params& p, double dt) {

@@ -68,6 +68,7 @@ Engine::Engine(int device) : dev(device) {
     LG_CK(cudaMallocHost(&pinned_small, 4096));
     tree = make_tree_state();
     adjoint = make_adjoint_state();
+    lets = make_let_store();
 }
 
 Engine::~Engine() {
@@ -75,6 +76,7 @@ Engine::~Engine() {
     if (stream) cudaStreamSynchronize(stream);
     tree.reset();
     adjoint.reset();
+    lets.reset();
     for (auto& ev : events) if (ev) cudaEventDestroy(ev);
     for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
     if (pinned_small) cudaFreeHost(pinned_small);
@@ -213,10 +215,10 @@ void Engine::build_tree(const lg_force_params& p) {
     pend_tree_times = true;
 }
 
-void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_t nremote) {
+void Engine::compute_forces_with(const lg_force_params& p, bool potential, const lg_let_tree* remote,
+                                 size_t nremote) {
     LG_CK(cudaSetDevice(dev));
-    if (nremote > 0)
-        fail(kRuntime, "cuda compute_forces_with: remote locally-essential trees are not supported by this engine");
+    if (nremote > 0 && !remote) fail(kArg, "compute_forces_with: null remote tree array");
     times.walk_ms = times.force_ms = 0;
     times.interactions = 0;
     costs_ok = false;
@@ -233,6 +235,9 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
     const float e2 = static_cast<float>(p.eps * p.eps);
     const bool eps0 = !(e2 >= 1.17549435e-38f);  // zero or denormal: guarded pair kernel
     LG_CK(cudaMemsetAsync(small.as<char>(), 0, 128, stream));
+    // Remote trees (other ranks' locally-essential trees) go to the device before the timed part.
+    const LetView let = nremote > 0 ? let_upload(*this, remote, nremote) : LetView{};
+    const bool have_let = let.ntrees > 0;
     LG_CK(cudaEventRecord(events[EV_WALK0], stream));
     BodyArrays b = bodies(cur);
     if (!tree_m) {
@@ -243,8 +248,10 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
         launches += slices > 1 ? 2 : 1;
         launch_fill_cost(b.cost, static_cast<float>(n - 1), n, stream);
         ++launches;
+        // Remote trees per block of 128 consecutive bodies (src/cpu_backend.cpp:695-717).
+        if (have_let) tree_walk_remote_blocks(*this, G, e2, potential, eps0, let, let_body_blocks(*this, 128));
     } else {
-        tree_walk(*this, G, e2, potential, eps0);
+        tree_walk(*this, G, e2, potential, eps0, nullptr, nullptr, have_let ? &let : nullptr);
     }
     LG_CK(cudaEventRecord(events[EV_WALK1], stream));
     LG_CK(cudaMemcpyAsync(pinned_small, small.as<char>(), 128, cudaMemcpyDeviceToHost, stream));
@@ -255,7 +262,7 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
         // walk again. The bodies are already sorted, so the stable re-sort keeps their order.
         LG_CK(cudaMemsetAsync(err_word(), 0, 4, stream));
         build_tree(p);
-        compute_forces_with(p, potential, nremote);
+        compute_forces_with(p, potential, remote, nremote);
         return;
     }
     check_device_errors(tree_m ? "cuda tree walk" : "cuda direct");
@@ -265,9 +272,10 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, size_
     times.walk_ms = elapsed(EV_WALK0, EV_WALK1);
     times.force_ms = times.sort_ms + times.build_ms + times.walk_ms;
     const unsigned long long* cnt = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(pinned_small) + 64);
-    // Walk: [0] body pairs (own entry excluded), [1] cell terms.
-    last_body_pairs = tree_m ? cnt[0] : static_cast<uint64_t>(n) * static_cast<uint64_t>(n - 1);
-    last_cell_terms = tree_m ? cnt[1] : 0;
+    // Walk: [0] body pairs (own entry excluded), [1] cell terms; the direct method adds its
+    // remote walk's entries to its n (n - 1) pairs.
+    last_body_pairs = tree_m ? cnt[0] : static_cast<uint64_t>(n) * static_cast<uint64_t>(n - 1) + cnt[0];
+    last_cell_terms = cnt[1];
     times.interactions = last_body_pairs + last_cell_terms;
     has_pe = potential;
     acc_ok = true;
@@ -530,7 +538,7 @@ lg_status lg_compute_forces(lg_engine* e, const lg_force_params* p, int potentia
         need(p, "params");
         Engine& E = eng(e);
         E.build_tree(*p);
-        E.compute_forces_with(*p, potential != 0, 0);
+        E.compute_forces_with(*p, potential != 0, nullptr, 0);
     });
 }
 
@@ -573,10 +581,33 @@ lg_status lg_build_tree(lg_engine* e, const lg_force_params* p) {
     });
 }
 
-lg_status lg_compute_forces_with(lg_engine* e, const lg_force_params* p, int potential, size_t nremote) {
+lg_status lg_compute_forces_with(lg_engine* e, const lg_force_params* p, int potential, const lg_let_tree* remote,
+                                 size_t nremote) {
     return guard([&] {
         need(p, "params");
-        eng(e).compute_forces_with(*p, potential != 0, nremote);
+        eng(e).compute_forces_with(*p, potential != 0, remote, nremote);
+    });
+}
+
+lg_status lg_export_let(lg_engine* e, const float lo[3], const float hi[3], const lg_force_params* p, size_t* nnodes,
+                        size_t* nbodies) {
+    return guard([&] {
+        need(lo, "lo");
+        need(hi, "hi");
+        need(p, "params");
+        need(nnodes, "nnodes");
+        need(nbodies, "nbodies");
+        Engine& E = eng(e);
+        LG_CK(cudaSetDevice(E.dev));
+        lg::let_export(E, lo, hi, *p, nnodes, nbodies);
+    });
+}
+
+lg_status lg_export_let_read(lg_engine* e, lg_let_node* nodes, float* bx, float* by, float* bz, float* bm) {
+    return guard([&] {
+        Engine& E = eng(e);
+        LG_CK(cudaSetDevice(E.dev));
+        lg::let_export_read(E, nodes, bx, by, bz, bm);
     });
 }
 

@@ -13,6 +13,7 @@ namespace lg {
 
 struct TreeState;     // tree.cu
 struct AdjointState;  // adjoint.cu
+struct LetStore;      // let.cu
 
 // Read-only view of the built tree for the walk.
 struct TreeView {
@@ -34,6 +35,21 @@ struct TreeView {
     size_t K;
 };
 
+// Remote (locally-essential) trees on the device, back to back: per node the centre of mass and
+// mass, the quadrupole (xx, xy, xz, yy) and (yz, zz, rcrit2, 0), and (first_child, child_count,
+// body_first, body_count) as indices into these arrays; bodies as (x, y, z, m); the roots of the
+// ntrees non-empty trees.
+struct LetView {
+    const float4* com = nullptr;
+    const float4* q0 = nullptr;
+    const float4* q1 = nullptr;
+    const int4* link = nullptr;
+    const float4* body = nullptr;
+    const uint32_t* roots = nullptr;
+    uint32_t nnodes = 0;
+    int ntrees = 0;
+};
+
 struct BodySet {
     DevBuf x, y, z, hm, lo, vx, vy, vz, m, cost, id;
 };
@@ -47,7 +63,7 @@ struct Engine {
                 const float* vz, const float* m, const uint32_t* id);
     void download(float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m, uint32_t* id);
     void build_tree(const lg_force_params& p);
-    void compute_forces_with(const lg_force_params& p, bool potential, size_t nremote);
+    void compute_forces_with(const lg_force_params& p, bool potential, const lg_let_tree* remote, size_t nremote);
     void kick(double dt);
     void drift(double dt);
     lg_diag diagnostics();
@@ -106,6 +122,7 @@ struct Engine {
     uint64_t last_body_pairs = 0, last_cell_terms = 0;
     std::unique_ptr<TreeState, void (*)(TreeState*)> tree{nullptr, nullptr};
     std::unique_ptr<AdjointState, void (*)(AdjointState*)> adjoint{nullptr, nullptr};
+    std::unique_ptr<LetStore, void (*)(LetStore*)> lets{nullptr, nullptr};
 };
 
 extern thread_local std::string g_last_error;
@@ -139,8 +156,20 @@ lg_memory_estimate memory_need(uint64_t n, int method);
 const void* probe_kernel();
 // walk.cu
 // sys/e2_sys: forest walk (per-body system, per-system squared softening); nullptr for one tree.
+// let: remote trees walked after the local one (nullptr: none).
 void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys = nullptr,
-               const float* e2_sys = nullptr);
+               const float* e2_sys = nullptr, const LetView* let = nullptr);
+// Remote trees only, for groups given by `blocks` (grp_range, grp_box, ngroups); adds to acc and
+// cost (the direct method's remote part).
+void tree_walk_remote_blocks(Engine& e, float G, float e2, bool potential, bool eps0, const LetView& let,
+                             const TreeView& blocks);
+// let.cu: remote trees to the device; blocks of consecutive bodies with their boxes; export.
+std::unique_ptr<LetStore, void (*)(LetStore*)> make_let_store();
+LetView let_upload(Engine& e, const lg_let_tree* remote, size_t nremote);
+TreeView let_body_blocks(Engine& e, int block);
+void let_export(Engine& e, const float lo[3], const float hi[3], const lg_force_params& p, size_t* nnodes,
+                size_t* nbodies);
+void let_export_read(Engine& e, lg_let_node* nodes, float* bx, float* by, float* bz, float* bm);
 // walk_vjp.cu: vector-Jacobian product of the tree forces over the current tree's interaction
 // lists (the lists are those of the force walk on the same tree), with the cell moments
 // differentiated through the bodies: g (4 arrays of n doubles: x, y, z, m; current body order)

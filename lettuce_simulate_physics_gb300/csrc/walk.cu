@@ -71,6 +71,11 @@ struct WalkArgs {
     // per-system squared softening; system s's tree is rooted at node s.
     const uint32_t* sys;
     const float* e2_sys;
+    // Remote trees walked after the local tree (or alone: local == 0, for the direct method's
+    // blocks of consecutive bodies); accumulate adds to acc and cost instead of overwriting.
+    LetView let;
+    int local;
+    int accumulate;
 };
 
 __device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
@@ -215,7 +220,14 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
         for (int k = lane; k < cc2; k += 32) {
             if (k < cc) {
                 const uint32_t nd = s.clist[c0 + k];
-                const float4 com = w.tv.nd_com[nd], cl = w.tv.nd_comlo[nd], q0 = w.tv.nd_q0[nd], q1 = w.tv.nd_q1[nd];
+                float4 com, cl, q0, q1;
+                if (nd & REMOTE) {
+                    const uint32_t r = nd & ~REMOTE;
+                    com = w.let.com[r]; q0 = w.let.q0[r]; q1 = w.let.q1[r];
+                    cl = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    com = w.tv.nd_com[nd]; cl = w.tv.nd_comlo[nd]; q0 = w.tv.nd_q0[nd]; q1 = w.tv.nd_q1[nd];
+                }
                 s.cx[k] = (com.x - ox) + cl.x;
                 s.cy[k] = (com.y - oy) + cl.y;
                 s.cz[k] = (com.z - oz) + cl.z;
@@ -238,7 +250,14 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
         for (int k = lane; k < bc2; k += 32) {
             if (k < bc) {
                 const uint32_t j = range_body(s, nr, b0 + k);
-                const float4 h = w.hm[j], l = w.lo[j];
+                float4 h, l;
+                if (j & REMOTE) {
+                    h = w.let.body[j & ~REMOTE];
+                    l = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    h = w.hm[j];
+                    l = w.lo[j];
+                }
                 s.bx[k] = (h.x - ox) + l.x;
                 s.by[k] = (h.y - oy) + l.y;
                 s.bz[k] = (h.z - oz) + l.z;
@@ -275,8 +294,14 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     const uint32_t root = w.sys ? w.sys[gr.x] : 0u;
     const float e2 = w.e2_sys ? w.e2_sys[root] : w.e2;
     uint32_t list_len = 0, cells_len = 0;
-    traverse(w.tv, s, stack, lane, gr, bc, bh, root, w.err, list_len, cells_len,
-             [&](int nc, int nr) { flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2); });
+    auto fl = [&](int nc, int nr) { flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2); };
+    if (w.local) traverse(w.tv, s, stack, lane, gr, bc, bh, root, w.err, list_len, cells_len, fl);
+    for (int t = 0; t < w.let.ntrees; ++t)
+        traverse_let(w.let, s, stack, lane, bc, bh, w.let.roots[t], w.err, list_len, cells_len, fl);
+    // With the local tree the own body is in the list (its leaf is inside the group, so it is
+    // opened): it is not an interaction, and with eps > 0 its pair (d = 0) only adds m_i/eps to the
+    // potential, which is taken out. Remote trees never hold the target.
+    const uint32_t self = w.local ? 1u : 0u;
     const float self_inv = (POT && !EPS0) ? rsqrt_mufu(e2) : 0.f;
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
@@ -285,14 +310,19 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         const uint32_t i = plo + k;
         const float* ks = &s.ks[u][0][lane];
         float p = ks[96] - ks[224];
-        // The own body is always in the list (its leaf is inside the group, so it is opened);
-        // with eps > 0 its pair has d = 0 and only adds m_i/eps to the potential.
-        if (POT && !EPS0) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
-        w.acc[i] = make_float4(w.G * (ks[0] - ks[128]), w.G * (ks[32] - ks[160]), w.G * (ks[64] - ks[192]),
-                               POT ? -w.G * p : 0.f);
-        w.cost[i] = static_cast<float>(list_len - 1);
+        if (POT && !EPS0 && w.local) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
+        const float4 a = make_float4(w.G * (ks[0] - ks[128]), w.G * (ks[32] - ks[160]), w.G * (ks[64] - ks[192]),
+                                     POT ? -w.G * p : 0.f);
+        if (w.accumulate) {
+            const float4 o = w.acc[i];
+            w.acc[i] = make_float4(o.x + a.x, o.y + a.y, o.z + a.z, o.w + a.w);
+            w.cost[i] += static_cast<float>(list_len);
+        } else {
+            w.acc[i] = a;
+            w.cost[i] = static_cast<float>(list_len - self);
+        }
     }
-    inter_b += static_cast<unsigned long long>(list_len - cells_len - 1) * static_cast<unsigned long long>(np);
+    inter_b += static_cast<unsigned long long>(list_len - cells_len - self) * static_cast<unsigned long long>(np);
     inter_c += static_cast<unsigned long long>(cells_len) * static_cast<unsigned long long>(np);
 }
 
@@ -337,21 +367,8 @@ int walk_blocks(int sms) {
 
 }  // namespace
 
-void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys, const float* e2_sys) {
-    WalkArgs w;
-    w.sys = sys;
-    w.e2_sys = e2_sys;
-    w.tv = tree_view(e);
-    BodyArrays b = e.bodies(e.cur);
-    w.hm = b.hm;
-    w.lo = b.lo;
-    w.acc = e.acc.as<float4>();
-    w.cost = b.cost;
-    w.group_ctr = reinterpret_cast<unsigned*>(e.small.as<char>() + 32);
-    w.inter = e.inter_counter();
-    w.err = e.err_word();
-    w.G = G;
-    w.e2 = e2;
+namespace {
+void launch_walk(Engine& e, WalkArgs& w, bool potential, bool eps0) {
     int blocks;
     if (potential) blocks = eps0 ? walk_blocks<true, true>(e.sms) : walk_blocks<true, false>(e.sms);
     else blocks = eps0 ? walk_blocks<false, true>(e.sms) : walk_blocks<false, false>(e.sms);
@@ -366,6 +383,49 @@ void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const ui
     }
     LG_LAUNCHED();
     ++e.launches;
+}
+}  // namespace
+
+void tree_walk_remote_blocks(Engine& e, float G, float e2, bool potential, bool eps0, const LetView& let,
+                             const TreeView& blocks) {
+    WalkArgs w{};
+    w.tv = blocks;
+    BodyArrays b = e.bodies(e.cur);
+    w.hm = b.hm;
+    w.lo = b.lo;
+    w.acc = e.acc.as<float4>();
+    w.cost = b.cost;
+    w.group_ctr = reinterpret_cast<unsigned*>(e.small.as<char>() + 36);
+    w.inter = e.inter_counter();
+    w.err = e.err_word();
+    w.G = G;
+    w.e2 = e2;
+    w.let = let;
+    w.local = 0;
+    w.accumulate = 1;
+    launch_walk(e, w, potential, eps0);
+}
+
+void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const uint32_t* sys, const float* e2_sys,
+               const LetView* let) {
+    WalkArgs w{};
+    w.sys = sys;
+    w.e2_sys = e2_sys;
+    if (let) w.let = *let;
+    w.local = 1;
+    w.accumulate = 0;
+    w.tv = tree_view(e);
+    BodyArrays b = e.bodies(e.cur);
+    w.hm = b.hm;
+    w.lo = b.lo;
+    w.acc = e.acc.as<float4>();
+    w.cost = b.cost;
+    w.group_ctr = reinterpret_cast<unsigned*>(e.small.as<char>() + 32);
+    w.inter = e.inter_counter();
+    w.err = e.err_word();
+    w.G = G;
+    w.e2 = e2;
+    launch_walk(e, w, potential, eps0);
 }
 
 }  // namespace lg

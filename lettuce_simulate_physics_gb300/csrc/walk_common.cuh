@@ -111,6 +111,93 @@ __device__ __forceinline__ void traverse(const TreeView& tv, S& s, uint32_t* sta
     if (overflow && lane == 0) atomicOr(err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
 }
 
+// List entries from a remote tree carry this bit (cell: node index; body range: first body).
+constexpr uint32_t REMOTE = 0x80000000u;
+
+// The receiver walk of a remote tree (src/backend.hpp:77-82, src/cpu_backend.cpp:787-812) for the
+// group box (bc, bh), warp-cooperative like traverse(): a node with no children and no bodies, or
+// whose box distance d satisfies d^2 >= rcrit2, is accepted (as bodies when it holds 1..SMALL_LEAF
+// of them, else as a multipole); otherwise its bodies, or else its children, are taken. Appends
+// to the same lists (entries flagged REMOTE) and flushes like traverse().
+template <class S, class F>
+__device__ __forceinline__ void traverse_let(const LetView& lv, S& s, uint32_t* stack, int lane, float4 bc, float4 bh,
+                                             uint32_t root, unsigned* err, uint32_t& list_len, uint32_t& cells_len,
+                                             F&& flush) {
+    const unsigned lt = (1u << lane) - 1u;
+    int sp = 1;
+    if (lane == 0) stack[0] = root;
+    __syncwarp();
+    int nc = 0, nr = 0, nbr = 0;
+    bool overflow = false;
+    const uint32_t max_iter = lv.nnodes + 64u;
+    uint32_t iter = 0;
+    for (;;) {
+        const bool done = sp == 0;
+        if (done || nc >= CL_FLUSH || nr >= RL_FLUSH || nbr >= BR_FLUSH) {
+            flush(nc, nr);
+            list_len += nc + nbr;
+            cells_len += nc;
+            nc = nr = nbr = 0;
+            if (done) break;
+        }
+        if (++iter > max_iter) {
+            overflow = true;
+            break;
+        }
+        const int take = min(32, sp);
+        sp -= take;
+        const bool have = lane < take;
+        const uint32_t node = have ? stack[sp + lane] : 0u;
+        __syncwarp();
+        int kind = 0;  // 1 cell, 2 bodies, 3 children
+        uint32_t a0 = 0, a1 = 0;
+        if (have && node >= lv.nnodes) {
+            atomicOr(err, kErrNodeOverflow);
+        } else if (have) {
+            const int4 L = lv.link[node];
+            const bool terminal = L.x < 0 && L.w == 0;
+            bool accept = terminal;
+            if (!terminal) {
+                const float4 com = lv.com[node];
+                const float rc2 = lv.q1[node].z;
+                const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.x, bc.x)), bh.x), 0.f);
+                const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.y, bc.y)), bh.y), 0.f);
+                const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.z, bc.z)), bh.z), 0.f);
+                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                accept = d2 >= rc2;
+            }
+            if (accept) {
+                if (L.w > 0 && L.w <= SMALL_LEAF) { kind = 2; a0 = REMOTE | static_cast<uint32_t>(L.z); a1 = L.w; }
+                else { kind = 1; a0 = REMOTE | node; }
+            } else if (L.w > 0) {
+                kind = 2; a0 = REMOTE | static_cast<uint32_t>(L.z); a1 = L.w;
+            } else if (L.y > 0) {
+                kind = 3; a0 = static_cast<uint32_t>(L.x); a1 = L.y;
+            }
+        }
+        const unsigned cm = __ballot_sync(0xffffffffu, kind == 1);
+        if (kind == 1) s.clist[nc + __popc(cm & lt)] = a0;
+        nc += __popc(cm);
+        const unsigned rm = __ballot_sync(0xffffffffu, kind == 2);
+        if (kind == 2) s.rlist[nr + __popc(rm & lt)] = make_uint2(a0, a1);
+        nr += __popc(rm);
+        int btot;
+        warp_excl_scan(kind == 2 ? static_cast<int>(a1) : 0, lane, btot);
+        nbr += btot;
+        int ctot;
+        const int coff = warp_excl_scan(kind == 3 ? static_cast<int>(a1) : 0, lane, ctot);
+        if (sp + ctot > SCAP) {
+            overflow = true;
+            break;
+        }
+        if (kind == 3)
+            for (uint32_t k = 0; k < a1; ++k) stack[sp + coff + k] = a0 + (a1 - 1 - k);  // first child on top
+        sp += ctot;
+        __syncwarp();
+    }
+    if (overflow && lane == 0) atomicOr(err, iter > max_iter ? kErrNodeOverflow : kErrStackOverflow);
+}
+
 // Prefix sums of the pending body ranges' lengths into s.rpre (nr <= RL_CAP); returns the total.
 template <class S>
 __device__ __forceinline__ int range_prefix(S& s, int nr, int lane) {

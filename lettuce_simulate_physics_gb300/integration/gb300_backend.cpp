@@ -8,10 +8,9 @@
 // std::runtime_error; make_cuda_backend returns nullptr and sets `why` when the engine is
 // unavailable.
 //
-// Locally-essential trees (the MPI layer's export_let / compute_forces_with(remote)) are outside
-// the engine. export_let is answered here on the host from the engine's tree, which is in the
-// reference CPU backend's node layout, with the receiver contract of src/backend.hpp:58-77;
-// compute_forces_with with remote trees throws.
+// Locally-essential trees (the MPI layer's export_let / compute_forces_with(remote)) are built and
+// walked on the device (lg_export_let, lg_compute_forces_with): LetNode and lg_let_node share one
+// layout, so the trees cross the boundary without conversion.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -60,7 +59,6 @@ public:
     void upload(const Bodies& b) override {
         ck(lg_upload(e_, b.size(), b.x.data(), b.y.data(), b.z.data(), b.vx.data(), b.vy.data(), b.vz.data(),
                      b.m.data(), b.id.data()));
-        tree_cache_ok_ = false;
     }
 
     void download(Bodies& b) override {
@@ -74,14 +72,12 @@ public:
     void compute_forces(const ForceParams& p, bool potential) override {
         const lg_force_params c = cparams(p);
         ck(lg_compute_forces(e_, &c, potential ? 1 : 0));
-        tree_cache_ok_ = false;
     }
 
     void kick(double dt) override { ck(lg_kick(e_, dt)); }
 
     void drift(double dt) override {
         ck(lg_drift(e_, dt));
-        tree_cache_ok_ = false;
     }
 
     Diag diagnostics() override {
@@ -119,64 +115,33 @@ public:
     void build_tree(const ForceParams& p) override {
         const lg_force_params c = cparams(p);
         ck(lg_build_tree(e_, &c));
-        tree_cache_ok_ = false;
-        built_method_ = p.method;
     }
 
     LetTree export_let(const Box3& target, const ForceParams& p) override {
         LetTree out;
-        size_t n = 0;
-        ck(lg_size(e_, &n));
-        if (n == 0) return out;
-        if (p.method == ForceMethod::direct) return export_direct();
-        load_tree();
-        if (nodes_.empty() || mom_[3] <= 0) return out;
-        const float bcx = 0.5f * (target.lo[0] + target.hi[0]), bhx = 0.5f * (target.hi[0] - target.lo[0]);
-        const float bcy = 0.5f * (target.lo[1] + target.hi[1]), bhy = 0.5f * (target.hi[1] - target.lo[1]);
-        const float bcz = 0.5f * (target.lo[2] + target.hi[2]), bhz = 0.5f * (target.hi[2] - target.lo[2]);
-        // Breadth-first: the output doubles as the queue, so each sibling set stays contiguous.
-        std::vector<uint32_t> src;
-        auto emit = [&](uint32_t ni) {
-            const float* m = &mom_[11 * ni];
-            LetNode l{};
-            l.cx = m[0]; l.cy = m[1]; l.cz = m[2]; l.mass = m[3];
-            l.qxx = m[4]; l.qxy = m[5]; l.qxz = m[6]; l.qyy = m[7]; l.qyz = m[8]; l.qzz = m[9];
-            l.rcrit2 = m[10];
-            l.first_child = -1; l.child_count = 0; l.body_first = -1; l.body_count = 0;
-            out.nodes.push_back(l);
-            src.push_back(ni);
-        };
-        emit(0);
-        for (size_t k = 0; k < out.nodes.size(); ++k) {
-            const uint32_t ni = src[k];
-            const float* m = &mom_[11 * ni];
-            const uint32_t* r = &range_[4 * ni];  // lo, hi, first, nchild
-            const float dx = std::max(std::fabs(m[0] - bcx) - bhx, 0.f);
-            const float dy = std::max(std::fabs(m[1] - bcy) - bhy, 0.f);
-            const float dz = std::max(std::fabs(m[2] - bcz) - bhz, 0.f);
-            if (dx * dx + dy * dy + dz * dz >= m[10]) continue;  // terminal
-            if (r[3] == 0) {
-                out.nodes[k].body_first = static_cast<int32_t>(out.bx.size());
-                out.nodes[k].body_count = static_cast<int32_t>(r[1] - r[0]);
-                for (uint32_t i = r[0]; i < r[1]; ++i) {
-                    out.bx.push_back(bodies_.x[i]); out.by.push_back(bodies_.y[i]);
-                    out.bz.push_back(bodies_.z[i]); out.bm.push_back(bodies_.m[i]);
-                }
-                continue;
-            }
-            const int32_t first = static_cast<int32_t>(out.nodes.size());
-            for (uint32_t c = r[2]; c < r[2] + r[3]; ++c)
-                if (mom_[11 * c + 3] > 0) emit(c);
-            out.nodes[k].first_child = first;
-            out.nodes[k].child_count = static_cast<int32_t>(out.nodes.size()) - first;
-        }
+        const lg_force_params c = cparams(p);
+        size_t nn = 0, nb = 0;
+        ck(lg_export_let(e_, target.lo, target.hi, &c, &nn, &nb));
+        out.nodes.resize(nn);
+        out.bx.resize(nb); out.by.resize(nb); out.bz.resize(nb); out.bm.resize(nb);
+        ck(lg_export_let_read(e_, reinterpret_cast<lg_let_node*>(out.nodes.data()), out.bx.data(), out.by.data(),
+                              out.bz.data(), out.bm.data()));
         return out;
     }
 
     void compute_forces_with(const ForceParams& p, bool potential,
                              const std::vector<const LetTree*>& remote) override {
         const lg_force_params c = cparams(p);
-        ck(lg_compute_forces_with(e_, &c, potential ? 1 : 0, remote.size()));
+        std::vector<lg_let_tree> trees(remote.size());
+        for (size_t k = 0; k < remote.size(); ++k) {
+            const LetTree& t = *remote[k];
+            lg_let_tree& d = trees[k];
+            d.nodes = reinterpret_cast<const lg_let_node*>(t.nodes.data());
+            d.nnodes = t.nodes.size();
+            d.bx = t.bx.data(); d.by = t.by.data(); d.bz = t.bz.data(); d.bm = t.bm.data();
+            d.nbodies = t.bx.size();
+        }
+        ck(lg_compute_forces_with(e_, &c, potential ? 1 : 0, trees.data(), trees.size()));
     }
 
     MemoryNeed memory_need(uint64_t n, ForceMethod m) const override {
@@ -204,48 +169,10 @@ public:
     }
 
 private:
-    // One always-open root holding every body (the reference's direct-method LET).
-    LetTree export_direct() {
-        LetTree out;
-        download(bodies_);
-        out.bx = bodies_.x; out.by = bodies_.y; out.bz = bodies_.z; out.bm = bodies_.m;
-        double M = 0, sx = 0, sy = 0, sz = 0;
-        for (size_t i = 0; i < bodies_.size(); ++i) {
-            const double m = bodies_.m[i];
-            M += m; sx += m * bodies_.x[i]; sy += m * bodies_.y[i]; sz += m * bodies_.z[i];
-        }
-        LetNode r{};
-        if (M > 0) { r.cx = float(sx / M); r.cy = float(sy / M); r.cz = float(sz / M); }
-        r.mass = float(M);
-        r.rcrit2 = 3.0e38f;
-        r.first_child = -1; r.child_count = 0;
-        r.body_first = 0; r.body_count = static_cast<int32_t>(bodies_.size());
-        out.nodes.push_back(r);
-        return out;
-    }
-
-    // The engine's tree after build_tree (reference node layout), cached until the next change.
-    void load_tree() {
-        if (tree_cache_ok_) return;
-        size_t nodes = 0, leaves = 0, groups = 0;
-        int depth = 0;
-        ck(lg_tree_counts(e_, &nodes, &leaves, &groups, &depth));
-        range_.resize(4 * nodes);
-        mom_.resize(11 * nodes);
-        ck(lg_tree_nodes(e_, range_.data(), mom_.data(), nullptr, nodes));
-        nodes_.assign(nodes, 0);
-        download(bodies_);
-        tree_cache_ok_ = true;
-    }
-
     lg_engine* e_;
-    bool tree_cache_ok_ = false;
-    ForceMethod built_method_ = ForceMethod::direct;
-    std::vector<uint32_t> range_;
-    std::vector<float> mom_;
-    std::vector<char> nodes_;
-    Bodies bodies_;
 };
+
+static_assert(sizeof(LetNode) == sizeof(lg_let_node), "LetNode and lg_let_node share one layout");
 
 }  // namespace
 

@@ -90,6 +90,11 @@ def _lib(kind: str) -> C.CDLL:
     }
     if kind == "port":
         sig["threads"] = (C.c_int, [vp])
+    else:
+        sig["export_let"] = (None, [vp, _f, _f, C.c_int, C.c_double, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)])
+        sig["export_let_read"] = (None, [vp, _f, _f, _f, _f])
+        sig["compute_forces_remote"] = (None, [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, vp,
+                                               C.c_size_t, _f, _f, _f, _f, C.c_size_t])
     for name, (res, args) in sig.items():
         fn = getattr(lib, p + name)
         fn.restype = res
@@ -208,6 +213,25 @@ class OracleBackend:
     def body_costs(self):
         c = np.zeros(len(self), np.float32)
         return c if self._call("body_costs", self._h, _fp(c)) else None
+
+    # ---- locally-essential trees (reference library only) ----
+    def export_let(self, lo, hi, method=TREE, theta=0.6):
+        """(nodes: 60-byte records as a uint8 (k, 60) array, bx, by, bz, bm) of the reference's export."""
+        lo = np.ascontiguousarray(lo, np.float32)
+        hi = np.ascontiguousarray(hi, np.float32)
+        nn, nb = C.c_size_t(), C.c_size_t()
+        self._call("export_let", self._h, _fp(lo), _fp(hi), int(method), float(theta), C.byref(nn), C.byref(nb))
+        nodes = np.zeros((nn.value, 60), np.uint8)
+        cols = [np.zeros(nb.value, np.float32) for _ in range(4)]
+        self._lib.ref_export_let_read(nodes.ctypes.data, *(_fp(c) for c in cols))
+        return nodes, cols
+
+    def compute_forces_remote(self, method, G, eps, theta, potential, nodes, cols):
+        nodes = np.ascontiguousarray(nodes, np.uint8)
+        cols = [np.ascontiguousarray(c, np.float32) for c in cols]
+        self._call("compute_forces_remote", self._h, int(method), float(G), float(eps), float(theta),
+                   int(bool(potential)), nodes.ctypes.data if len(nodes) else None, len(nodes),
+                   *(_fp(c) for c in cols), len(cols[0]))
 
     # ---- tree introspection ----
     def keys(self):

@@ -100,6 +100,38 @@ int ref_body_costs(void* h, float* cost) {
     return 1;
 }
 
+// Locally-essential trees through the reference's own export_let / compute_forces_with. The last
+// export is kept in the shim until the next one; LetNode is copied out as its 60 raw bytes.
+static LetTree g_last_let;
+
+void ref_export_let(void* h, const float* lo, const float* hi, int method, double theta, size_t* nnodes,
+                    size_t* nbodies) {
+    Box3 box;
+    for (int c = 0; c < 3; ++c) { box.lo[c] = lo[c]; box.hi[c] = hi[c]; }
+    g_last_let = as_cpu(h)->export_let(box, params(method, 1, 0.01, theta));
+    *nnodes = g_last_let.nodes.size();
+    *nbodies = g_last_let.bx.size();
+}
+
+void ref_export_let_read(void* nodes60, float* bx, float* by, float* bz, float* bm) {
+    std::memcpy(nodes60, g_last_let.nodes.data(), g_last_let.nodes.size() * sizeof(LetNode));
+    const size_t nb = g_last_let.bx.size();
+    std::memcpy(bx, g_last_let.bx.data(), nb * 4); std::memcpy(by, g_last_let.by.data(), nb * 4);
+    std::memcpy(bz, g_last_let.bz.data(), nb * 4); std::memcpy(bm, g_last_let.bm.data(), nb * 4);
+}
+
+// compute_forces_with(p, potential, {one remote tree given as raw arrays}).
+void ref_compute_forces_remote(void* h, int method, double G, double eps, double theta, int potential,
+                               const void* nodes60, size_t nnodes, const float* bx, const float* by, const float* bz,
+                               const float* bm, size_t nbodies) {
+    LetTree t;
+    t.nodes.resize(nnodes);
+    std::memcpy(t.nodes.data(), nodes60, nnodes * sizeof(LetNode));
+    t.bx.assign(bx, bx + nbodies); t.by.assign(by, by + nbodies); t.bz.assign(bz, bz + nbodies);
+    t.bm.assign(bm, bm + nbodies);
+    as_cpu(h)->compute_forces_with(params(method, G, eps, theta), potential != 0, {&t});
+}
+
 size_t ref_num_nodes(void* h) { return as_cpu(h)->nodes_.size(); }
 size_t ref_num_groups(void* h) { return as_cpu(h)->groups_.size(); }
 size_t ref_num_leaves(void* h) { return as_cpu(h)->leaves_.size(); }

@@ -1,6 +1,7 @@
 """Generates the golden vectors in this directory from the reference's own CPU backend.
 
-Run here, where the reference sources are present:  python tests/golden/make_golden.py
+Run here, where the reference sources are present:  python tests/golden/make_golden.py [prefix ...]
+(with prefixes, only the fixtures whose names start with one of them are written).
 It builds oracle/_ref/libref_cpu.so (the reference's src/cpu_backend.cpp, compiled unmodified by
 oracle/Makefile) and records, for seeded inputs, what the reference computes: Morton keys, the
 sort permutation, the octree (nodes, cells, groups, leaves), direct and tree accelerations and
@@ -65,7 +66,12 @@ def force_case(b, method, G, eps, theta, potential):
     return out
 
 
+ONLY: list[str] = []
+
+
 def save(name, inputs, params, **cases):
+    if ONLY and not any(name.startswith(o) for o in ONLY):
+        return
     rec = _bodies_fields("in_", inputs)
     for k, v in params.items():
         rec[f"param_{k}"] = np.asarray(v)
@@ -78,6 +84,7 @@ def save(name, inputs, params, **cases):
 
 
 def main():
+    ONLY.extend(sys.argv[1:])
     O.build(quiet=False)
     G = 1.0
     # Direct, Plummer 4096 (tests/test_cuda_backend.cpp:180-198 shape).
@@ -121,6 +128,33 @@ def main():
         b = S.cube(n, 100 + n)
         save(f"small_n{n}", b, dict(G=G, eps=0.05), direct=force_case(b, O.DIRECT, G, 0.05, 0.0, True),
              tree=force_case(b, O.TREE, G, 0.05, 0.0, True))
+    # Locally-essential trees (tests/test_cuda_let.cpp shapes): Plummer 8000 split at x = 0; the
+    # x >= 0 half exports for the x < 0 half's box (tree theta 0.6, and direct); the x < 0 half
+    # receives it (its own forces plus the remote tree).
+    b = S.plummer(8000, 17, cut=20)
+    left = b.x < 0
+    h0, h1 = b.subset(left), b.subset(~left)
+    lo = np.array([h0.x.min(), h0.y.min(), h0.z.min()], np.float32)
+    hi = np.array([h0.x.max(), h0.y.max(), h0.z.max()], np.float32)
+    cases = {}
+    for cname, method in (("tree", O.TREE), ("direct", O.DIRECT)):
+        ex = O.OracleBackend("ref", 0)
+        ex.upload(h1)
+        ex.build_tree(method, 0.6)
+        nodes, cols = ex.export_let(lo, hi, method, 0.6)
+        ex.close()
+        rx = O.OracleBackend("ref", 0)
+        rx.upload(_zero_v(h0))
+        rx.build_tree(method, 0.6)
+        rx.compute_forces_remote(method, G, 0.01, 0.6, True, nodes, cols)
+        dn = rx.download()
+        c = rx.body_costs()
+        cases[cname] = dict(let_nodes=nodes, let_bx=cols[0], let_by=cols[1], let_bz=cols[2], let_bm=cols[3],
+                            order_id=dn.id, acc=rx.accel(), interactions=np.uint64(rx.times()["interactions"]),
+                            costs=c if c is not None else np.zeros(0, np.float32))
+        rx.close()
+    save("let_plummer8000", h0, dict(G=G, eps=0.01, theta=0.6, box_lo=lo, box_hi=hi),
+         exporter=_bodies_fields("", h1), **cases)
     # KDK step sequence with diagnostics (:290-343 shape): force, kick, drift, force, kick.
     b = S.plummer(2000, 4, cut=20)
     be = O.OracleBackend("ref", 0)

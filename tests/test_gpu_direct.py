@@ -173,5 +173,11 @@ def test_state_errors_and_empty_and_single(be):
     be.upload(S.cube(1, 1))
     be.compute_forces(params(1, 0.01), True)
     assert be.diagnostics().pe == 0
-    with pytest.raises(RuntimeError):
+    with pytest.raises(TypeError):
         be.compute_forces_with(params(0, 0.01), False, remote=[object()])
+    # A remote tree whose links leave it is rejected before anything reaches the device.
+    bad = L.LetTree(np.zeros(1, L.backend.LET_NODE_DTYPE))
+    bad.nodes["first_child"] = 5
+    bad.nodes["child_count"] = 2
+    with pytest.raises(ValueError):
+        be.compute_forces_with(params(0, 0.01), False, remote=[bad])
