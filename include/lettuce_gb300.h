@@ -159,6 +159,35 @@ lg_status lg_body_costs(lg_engine* e, float* cost, size_t n, int* valid);
 
 /* ---- Extensions: no counterpart in the reference interface ------------------------------------ */
 
+/* RenderOptions, src/render.hpp:15-21: view "xy" | "xz" | "yz" | "<yaw_deg>,<pitch_deg>";
+ * extent = half-width in world units (0: 1.2 x the 99th-percentile radius about the centre of
+ * mass); color 0 = density, 1 = speed. */
+typedef struct {
+    int32_t width, height;
+    const char* view;
+    double extent;
+    int32_t color;
+    int32_t reserved;
+} lg_render_options;
+
+/* render_image(bodies, options), src/render.hpp:28-33 (src/render.cpp:83-224), on the device from
+ * the resident bodies: mass splatted bilinearly into a float image (integer sums: independent of
+ * atomic order), log tone map, the reference's colour ramps. rgb: width * height * 3 bytes, row 0
+ * at the top; *extent_used = the half-width used. No graphics API is involved: the image is a
+ * plain device buffer copied to rgb. */
+lg_status lg_render(lg_engine* e, const lg_render_options* o, unsigned char* rgb, double* extent_used);
+
+/* FP64-preserving restart (no reference counterpart). lg_upload64 is lg_upload with FP64 positions.
+ * A float snapshot (the reference's .snap, src/snapshot.hpp:1-27) loses the FP64 state; the sidecar
+ * written next to it by lg_write_fp64_sidecar holds, in download order, the ids and the low parts
+ * x - (double)(float)x (exact in FP64). lg_read_fp64_sidecar checks n and the ids against the
+ * snapshot's bodies and rebuilds the FP64 positions bit for bit (host only, no engine). */
+lg_status lg_upload64(lg_engine* e, size_t n, const double* x, const double* y, const double* z, const float* vx,
+                      const float* vy, const float* vz, const float* m, const uint32_t* id);
+lg_status lg_write_fp64_sidecar(lg_engine* e, const char* path, uint64_t step);
+lg_status lg_read_fp64_sidecar(const char* path, size_t n, const uint32_t* id, const float* x, const float* y,
+                               const float* z, double* x64, double* y64, double* z64, uint64_t* step);
+
 /* Accelerations and potential in the current body order (the reference tests read them through
  * kick(1) on zero velocities; this reads them directly). pot may be NULL. */
 lg_status lg_read_accel(lg_engine* e, float* ax, float* ay, float* az, float* pot);

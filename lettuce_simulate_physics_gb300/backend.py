@@ -138,6 +138,11 @@ class LetTree:
     bm: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
 
 
+class _CRenderOptions(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("view", C.c_char_p), ("extent", C.c_double),
+                ("color", C.c_int32), ("reserved", C.c_int32)]
+
+
 class _CLetTree(C.Structure):
     _fields_ = [("nodes", C.c_void_p), ("nnodes", C.c_size_t), ("bx", C.POINTER(C.c_float)),
                 ("by", C.POINTER(C.c_float)), ("bz", C.POINTER(C.c_float)), ("bm", C.POINTER(C.c_float)),
@@ -184,6 +189,10 @@ def _lib() -> C.CDLL:
         "lg_compute_forces_with": (st, [vp, C.POINTER(_CForceParams), C.c_int, C.POINTER(_CLetTree), C.c_size_t]),
         "lg_export_let": (st, [vp, _f, _f, C.POINTER(_CForceParams), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
         "lg_export_let_read": (st, [vp, C.c_void_p, _f, _f, _f, _f]),
+        "lg_upload64": (st, [vp, C.c_size_t, _d, _d, _d, _f, _f, _f, _f, _u]),
+        "lg_render": (st, [vp, C.POINTER(_CRenderOptions), C.POINTER(C.c_ubyte), _d]),
+        "lg_write_fp64_sidecar": (st, [vp, C.c_char_p, C.c_uint64]),
+        "lg_read_fp64_sidecar": (st, [C.c_char_p, C.c_size_t, _u, _f, _f, _f, _d, _d, _d, C.POINTER(C.c_uint64)]),
         "lg_memory_need": (st, [C.c_uint64, C.c_int, C.POINTER(_CMem)]),
         "lg_device_memory": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "lg_body_costs": (st, [vp, _f, C.c_size_t, C.POINTER(C.c_int)]),
@@ -256,6 +265,16 @@ def _cparams(p: ForceParams) -> _CForceParams:
     return _CForceParams(float(p.G), float(p.eps), float(p.theta), int(p.method), 0)
 
 
+def read_fp64_sidecar(path: str, b: Bodies):
+    """FP64 positions (n, 3) of the snapshot bodies b from their sidecar, and the step it records."""
+    n = len(b)
+    out = np.zeros((3, max(n, 1)), np.float64)
+    step = C.c_uint64()
+    _check(_lib().lg_read_fp64_sidecar(os.fsencode(path), n, _up(b.id), _fp(b.x), _fp(b.y), _fp(b.z),
+                                       *(out[k].ctypes.data_as(_d) for k in range(3)), C.byref(step)))
+    return out[:, :n].T.copy(), int(step.value)
+
+
 def cuda_compiled() -> bool:
     return bool(_lib().lg_compiled())
 
@@ -300,6 +319,25 @@ class CudaBackend:
     def upload(self, b: Bodies) -> None:
         _check(self._lib.lg_upload(self._h, len(b), _fp(b.x), _fp(b.y), _fp(b.z), _fp(b.vx), _fp(b.vy), _fp(b.vz),
                                    _fp(b.m), _up(b.id)))
+
+    def upload64(self, b: Bodies, pos64) -> None:
+        """upload with FP64 positions pos64 (n, 3) (b's positions are ignored)."""
+        p = np.ascontiguousarray(np.asarray(pos64, np.float64).reshape(len(b), 3).T)
+        _check(self._lib.lg_upload64(self._h, len(b), *(p[k].ctypes.data_as(_d) for k in range(3)), _fp(b.vx),
+                                     _fp(b.vy), _fp(b.vz), _fp(b.m), _up(b.id)))
+
+    def render(self, width: int = 1024, height: int = 1024, view: str = "xy", extent: float = 0.0,
+               color: str = "density"):
+        """Density render of the resident bodies (render_image): ((height, width, 3) uint8, extent)."""
+        o = _CRenderOptions(int(width), int(height), view.encode(), float(extent), 1 if color == "speed" else 0, 0)
+        rgb = np.zeros((int(height), int(width), 3), np.uint8)
+        ext = C.c_double()
+        _check(self._lib.lg_render(self._h, C.byref(o), rgb.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(ext)))
+        return rgb, float(ext.value)
+
+    def write_fp64_sidecar(self, path: str, step: int = 0) -> None:
+        """The low parts of the FP64 positions, in download order, next to a float snapshot."""
+        _check(self._lib.lg_write_fp64_sidecar(self._h, os.fsencode(path), int(step)))
 
     def size(self) -> int:
         n = C.c_size_t()

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -136,6 +137,26 @@ void Engine::upload(size_t count, const float* x, const float* y, const float* z
     // A kick before the first force call adds zero rather than garbage.
     LG_CK(cudaMemsetAsync(acc.as<float4>(), 0, count * 16, stream));
     LG_CK(cudaMemsetAsync(b.cost, 0, fb, stream));
+    LG_CK(cudaStreamSynchronize(stream));
+}
+
+void Engine::upload64(size_t count, const double* x, const double* y, const double* z, const float* vx,
+                      const float* vy, const float* vz, const float* m, const uint32_t* id) {
+    std::vector<float> f(count * 3);
+    for (size_t i = 0; i < count; ++i) {
+        f[i] = static_cast<float>(x[i]);
+        f[count + i] = static_cast<float>(y[i]);
+        f[2 * count + i] = static_cast<float>(z[i]);
+    }
+    upload(count, f.data(), f.data() + count, f.data() + 2 * count, vx, vy, vz, m, id);
+    if (n == 0) return;
+    const BodyArrays b = bodies(cur);
+    const size_t db = count * 8;
+    LG_CK(cudaMemcpyAsync(b.x, x, db, cudaMemcpyHostToDevice, stream));
+    LG_CK(cudaMemcpyAsync(b.y, y, db, cudaMemcpyHostToDevice, stream));
+    LG_CK(cudaMemcpyAsync(b.z, z, db, cudaMemcpyHostToDevice, stream));
+    launch_refresh_hilo(b, n, stream);
+    ++launches;
     LG_CK(cudaStreamSynchronize(stream));
 }
 
@@ -516,6 +537,78 @@ lg_status lg_upload(lg_engine* e, size_t n, const float* x, const float* y, cons
     });
 }
 
+lg_status lg_upload64(lg_engine* e, size_t n, const double* x, const double* y, const double* z, const float* vx,
+                      const float* vy, const float* vz, const float* m, const uint32_t* id) {
+    return guard([&] {
+        if (n) { need(x, "x"); need(y, "y"); need(z, "z"); need(vx, "vx"); need(vy, "vy"); need(vz, "vz");
+                 need(m, "m"); need(id, "id"); }
+        eng(e).upload64(n, x, y, z, vx, vy, vz, m, id);
+    });
+}
+
+// ---- FP64 sidecar of a float snapshot --------------------------------------------------------
+// Layout (little-endian): "LGF64LO1", u64 n, u64 step, u64 reserved, then u32 id[n] padded to 8
+// bytes, then f64 lo_x[n], lo_y[n], lo_z[n] with lo = x - (double)(float)x, exact in FP64, so
+// float + lo restores the position bit for bit. Written to <path>.tmp and renamed into place.
+lg_status lg_write_fp64_sidecar(lg_engine* e, const char* path, uint64_t step) {
+    return guard([&] {
+        need(path, "path");
+        Engine& E = eng(e);
+        const size_t n = static_cast<size_t>(E.n);
+        std::vector<double> p(3 * n);
+        std::vector<float> f(8 * n + 8);
+        std::vector<uint32_t> id(n + 2, 0);
+        if (n) {
+            E.read_pos64(p.data(), p.data() + n, p.data() + 2 * n);
+            E.download(f.data(), f.data() + n, f.data() + 2 * n, f.data() + 3 * n, f.data() + 4 * n, f.data() + 5 * n,
+                       f.data() + 6 * n, id.data());
+        }
+        for (size_t k = 0; k < 3 * n; ++k) p[k] -= static_cast<double>(static_cast<float>(p[k]));
+        const std::string tmp = std::string(path) + ".tmp";
+        FILE* fp = std::fopen(tmp.c_str(), "wb");
+        if (!fp) lg::fail(lg::kRuntime, std::string("cannot write ") + tmp);
+        const uint64_t hdr[3] = {n, step, 0};
+        bool ok = std::fwrite("LGF64LO1", 1, 8, fp) == 8 && std::fwrite(hdr, 8, 3, fp) == 3;
+        const size_t nid = (n + 1) & ~size_t(1);
+        ok = ok && std::fwrite(id.data(), 4, nid, fp) == nid;
+        ok = ok && (n == 0 || std::fwrite(p.data(), 8, 3 * n, fp) == 3 * n);
+        ok = (std::fclose(fp) == 0) && ok;
+        if (!ok || std::rename(tmp.c_str(), path) != 0) {
+            std::remove(tmp.c_str());
+            lg::fail(lg::kRuntime, std::string("writing ") + path + " failed");
+        }
+    });
+}
+
+lg_status lg_read_fp64_sidecar(const char* path, size_t n, const uint32_t* id, const float* x, const float* y,
+                               const float* z, double* x64, double* y64, double* z64, uint64_t* step) {
+    return guard([&] {
+        need(path, "path");
+        if (n) { need(id, "id"); need(x, "x"); need(y, "y"); need(z, "z"); need(x64, "x64"); need(y64, "y64");
+                 need(z64, "z64"); }
+        FILE* fp = std::fopen(path, "rb");
+        if (!fp) lg::fail(lg::kRuntime, std::string("cannot read ") + path);
+        char magic[8];
+        uint64_t hdr[3];
+        bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, "LGF64LO1", 8) == 0 &&
+                  std::fread(hdr, 8, 3, fp) == 3 && hdr[0] == n;
+        std::vector<uint32_t> fid(((n + 1) & ~size_t(1)) + 2);
+        std::vector<double> lo(3 * n);
+        const size_t nid = (n + 1) & ~size_t(1);
+        ok = ok && std::fread(fid.data(), 4, nid, fp) == nid && (n == 0 || std::fread(lo.data(), 8, 3 * n, fp) == 3 * n);
+        std::fclose(fp);
+        if (!ok) lg::fail(lg::kRuntime, std::string(path) + ": not an FP64 sidecar for " + std::to_string(n) + " bodies");
+        for (size_t i = 0; i < n; ++i)
+            if (fid[i] != id[i]) lg::fail(lg::kRuntime, std::string(path) + ": body order differs from the snapshot's");
+        for (size_t i = 0; i < n; ++i) {
+            x64[i] = static_cast<double>(x[i]) + lo[i];
+            y64[i] = static_cast<double>(y[i]) + lo[n + i];
+            z64[i] = static_cast<double>(z[i]) + lo[2 * n + i];
+        }
+        if (step) *step = hdr[1];
+    });
+}
+
 lg_status lg_size(const lg_engine* e, size_t* n) {
     return guard([&] {
         need(n, "n");
@@ -608,6 +701,16 @@ lg_status lg_export_let_read(lg_engine* e, lg_let_node* nodes, float* bx, float*
         Engine& E = eng(e);
         LG_CK(cudaSetDevice(E.dev));
         lg::let_export_read(E, nodes, bx, by, bz, bm);
+    });
+}
+
+lg_status lg_render(lg_engine* e, const lg_render_options* o, unsigned char* rgb, double* extent_used) {
+    return guard([&] {
+        need(o, "options");
+        need(rgb, "rgb");
+        Engine& E = eng(e);
+        LG_CK(cudaSetDevice(E.dev));
+        lg::render(E, *o, rgb, extent_used);
     });
 }
 

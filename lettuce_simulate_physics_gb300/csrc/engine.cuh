@@ -61,6 +61,8 @@ struct Engine {
     // Backend semantics (src/backend.hpp:89-141).
     void upload(size_t count, const float* x, const float* y, const float* z, const float* vx, const float* vy,
                 const float* vz, const float* m, const uint32_t* id);
+    void upload64(size_t count, const double* x, const double* y, const double* z, const float* vx, const float* vy,
+                  const float* vz, const float* m, const uint32_t* id);
     void download(float* x, float* y, float* z, float* vx, float* vy, float* vz, float* m, uint32_t* id);
     void build_tree(const lg_force_params& p);
     void compute_forces_with(const lg_force_params& p, bool potential, const lg_let_tree* remote, size_t nremote);
@@ -186,6 +188,8 @@ void adjoint_forward(Engine& e, AdjointState& a, const lg_force_params& p, doubl
 // tx, ty, tz: the target x* (loss sum m |x_T - x*|^2), or with seeded the caller's dL/dx_T (by id).
 double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const double* ty, const double* tz, double* gx,
                         double* gy, double* gz, double* gvx, double* gvy, double* gvz, double* gm, bool seeded);
+// render.cu
+void render(Engine& e, const lg_render_options& o, unsigned char* rgb, double* extent_used);
 // integrate.cu
 double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink);
 

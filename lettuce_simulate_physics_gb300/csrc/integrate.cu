@@ -39,6 +39,13 @@ __global__ void k_widen(const float* __restrict__ x, const float* __restrict__ y
     store_hilo(b, i, px, py, pz, m[i]);
 }
 
+// hi/lo split and masses into hm from the FP64 positions already in b (FP64 upload).
+__global__ void k_refresh_hilo(BodyArrays b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    store_hilo(b, i, b.x[i], b.y[i], b.z[i], b.m[i]);
+}
+
 __global__ void k_round_pos(const BodyArrays b, float* __restrict__ x, float* __restrict__ y, float* __restrict__ z,
                             int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -334,6 +341,12 @@ double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink) {
 void launch_widen(const float* x, const float* y, const float* z, const float* m, BodyArrays b, int n, cudaStream_t s) {
     if (n <= 0) return;
     k_widen<<<grid_for(n, BS), BS, 0, s>>>(x, y, z, m, b, n);
+    LG_LAUNCHED();
+}
+
+void launch_refresh_hilo(BodyArrays b, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_refresh_hilo<<<grid_for(n, BS), BS, 0, s>>>(b, n);
     LG_LAUNCHED();
 }
 

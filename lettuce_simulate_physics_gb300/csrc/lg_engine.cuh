@@ -41,6 +41,8 @@ struct DirectShape {
 // integrate.cu
 void launch_widen(const float* x, const float* y, const float* z, const float* m, BodyArrays b, int n,
                   cudaStream_t s);
+// hm/lo from the FP64 positions and masses already stored in b.
+void launch_refresh_hilo(BodyArrays b, int n, cudaStream_t s);
 void launch_round_pos(const BodyArrays b, float* x, float* y, float* z, int n, cudaStream_t s);
 void launch_kick(BodyArrays b, const float4* acc, float dt, int n, cudaStream_t s);
 void launch_drift(BodyArrays b, double dt, int n, cudaStream_t s);

@@ -304,6 +304,20 @@ def loss_direct_fp64(x0, v0, m, G, eps, dt, steps, xstar, threads=0):
                                    int(steps), _dp(xstar), int(threads))
 
 
+def render_ref(b, width, height, view="xy", extent=0.0, color=0):
+    """The reference's render_image (src/render.cpp) through oracle/_ref: ((h, w, 3) uint8, extent)."""
+    lib = _lib("ref")
+    fn = lib.ref_render
+    fn.restype = None
+    fn.argtypes = [C.c_size_t, _f, _f, _f, _f, _f, _f, _f, C.c_int, C.c_int, C.c_char_p, C.c_double, C.c_int,
+                   C.POINTER(C.c_ubyte), _d]
+    rgb = np.zeros((int(height), int(width), 3), np.uint8)
+    ext = C.c_double()
+    fn(len(b), _fp(b.x), _fp(b.y), _fp(b.z), _fp(b.vx), _fp(b.vy), _fp(b.vz), _fp(b.m), int(width), int(height),
+       view.encode(), float(extent), int(color), rgb.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(ext))
+    return rgb, float(ext.value)
+
+
 class FrozenTree:
     """FP64 tree forces over frozen interaction lists for a trajectory (or_frozen_*): `calls` is a
     list, one per force call s = 0 .. steps-1, of dicts with the engine's tree after that call:

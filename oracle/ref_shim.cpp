@@ -26,6 +26,8 @@
 #include "cpu_backend.cpp"
 #undef private
 
+#include "render.hpp"
+
 namespace {
 CpuBackend* as_cpu(void* h) { return static_cast<CpuBackend*>(h); }
 }  // namespace
@@ -130,6 +132,22 @@ void ref_compute_forces_remote(void* h, int method, double G, double eps, double
     t.bx.assign(bx, bx + nbodies); t.by.assign(by, by + nbodies); t.bz.assign(bz, bz + nbodies);
     t.bm.assign(bm, bm + nbodies);
     as_cpu(h)->compute_forces_with(params(method, G, eps, theta), potential != 0, {&t});
+}
+
+// The reference's render_image (src/render.cpp) on the given bodies; rgb: w * h * 3 bytes.
+void ref_render(size_t n, const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                const float* vz, const float* m, int w, int h, const char* view, double extent, int color,
+                unsigned char* rgb, double* extent_used) {
+    Bodies b;
+    b.x.assign(x, x + n); b.y.assign(y, y + n); b.z.assign(z, z + n);
+    b.vx.assign(vx, vx + n); b.vy.assign(vy, vy + n); b.vz.assign(vz, vz + n);
+    b.m.assign(m, m + n); b.id.resize(n);
+    RenderOptions o;
+    o.width = w; o.height = h; o.view = view; o.extent = extent;
+    o.color = color == 1 ? ColorMode::speed : ColorMode::density;
+    Image img = render_image(b, o);
+    std::memcpy(rgb, img.rgb.data(), img.rgb.size());
+    *extent_used = img.extent;
 }
 
 size_t ref_num_nodes(void* h) { return as_cpu(h)->nodes_.size(); }

@@ -155,6 +155,16 @@ def main():
         rx.close()
     save("let_plummer8000", h0, dict(G=G, eps=0.01, theta=0.6, box_lo=lo, box_hi=hi),
          exporter=_bodies_fields("", h1), **cases)
+    # Density renders (src/render.cpp render_image): a disk with its rotation velocities and a
+    # Plummer sphere, several views, fitted and fixed extents, density and speed colouring.
+    for name, b in (("render_disk20000", S.disk(20000, 5)), ("render_plummer5000", S.plummer(5000, 6, cut=20))):
+        cases = {}
+        for cname, (w, h, view, ext, color) in {"xy": (256, 256, "xy", 0.0, 0), "tilt": (200, 160, "30,60", 0.0, 1),
+                                                 "xz": (128, 128, "xz", 3.0, 0)}.items():
+            rgb, used = O.render_ref(b, w, h, view, ext, color)
+            cases[cname] = dict(rgb=rgb, extent=np.float64(used), width=np.int32(w), height=np.int32(h),
+                                view=np.array(view), extent_in=np.float64(ext), color=np.int32(color))
+        save(name, b, dict(G=G), **cases)
     # KDK step sequence with diagnostics (:290-343 shape): force, kick, drift, force, kick.
     b = S.plummer(2000, 4, cut=20)
     be = O.OracleBackend("ref", 0)

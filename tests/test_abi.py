@@ -72,3 +72,35 @@ def test_bodies_validation():
     with pytest.raises(ValueError):
         L.Bodies(np.zeros(3), np.zeros(2), np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(3),
                  np.zeros(3, np.uint32))
+
+
+def _write_sidecar(path, n, step, ids, lo):
+    with open(path, "wb") as f:
+        f.write(b"LGF64LO1")
+        f.write(np.array([n, step, 0], np.uint64).tobytes())
+        pad = np.zeros((n + 1) & ~1, np.uint32)
+        pad[:n] = ids
+        f.write(pad.tobytes())
+        f.write(np.ascontiguousarray(lo, np.float64).tobytes())
+
+
+def test_fp64_sidecar_reader(lib, tmp_path):
+    """The sidecar restores FP64 positions from a float snapshot bit for bit (host-only reader)."""
+    from lettuce_simulate_physics_gb300.backend import read_fp64_sidecar
+    rng = np.random.Generator(np.random.PCG64(5))
+    n = 1001
+    pos = rng.normal(0, 3, (n, 3))
+    ids = rng.permutation(n).astype(np.uint32)
+    f32 = pos.astype(np.float32)
+    lo = (pos - f32.astype(np.float64)).T  # (3, n) exact
+    path = str(tmp_path / "s.f64lo")
+    _write_sidecar(path, n, 77, ids, lo)
+    b = L.Bodies(f32[:, 0], f32[:, 1], f32[:, 2], np.zeros(n), np.zeros(n), np.zeros(n), np.ones(n), ids)
+    got, step = read_fp64_sidecar(path, b)
+    assert step == 77 and np.array_equal(got, pos)
+    bad = b.copy()
+    bad.id = bad.id[::-1].copy()
+    with pytest.raises(RuntimeError):
+        read_fp64_sidecar(path, bad)
+    with pytest.raises(RuntimeError):
+        read_fp64_sidecar(path, b.subset(np.arange(n - 1)))
