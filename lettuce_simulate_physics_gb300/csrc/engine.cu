@@ -52,6 +52,17 @@ Engine::Engine(int device) : dev(device) {
         group_max = static_cast<int>(v);
     }
     if (walk_body) group_max = 1;
+    if (const char* m = std::getenv("LETTUCE_GB300_WALK_GROUPS")) {
+        const std::string v = m;
+        if (v != "merged" && v != "reference")
+            fail(kRuntime, "LETTUCE_GB300_WALK_GROUPS must be merged or reference, not '" + v + "'");
+        walk_merge = v == "merged";
+    }
+    if (const char* c = std::getenv("LETTUCE_GB300_WALK_MERGE_CAP")) {
+        const int v = std::atoi(c);
+        if (v < 1 || v > 1024) fail(kRuntime, "LETTUCE_GB300_WALK_MERGE_CAP must be in [1, 1024]");
+        merge_cap = v;
+    }
     // Direct launch shape override "ipt,slices" (tuning; otherwise chosen per size).
     if (const char* d = std::getenv("LETTUCE_GB300_DIRECT")) {
         int ipt = 0, slices = 0;
@@ -60,6 +71,7 @@ Engine::Engine(int device) : dev(device) {
         direct_shape_override = DirectShape{ipt, 256, slices};
     }
     name += walk_body ? ", per-body walk" : ", group walk " + std::to_string(group_max);
+    if (!walk_body) name += walk_merge ? " (packed)" : " (reference groups)";
     LG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& ev : events) LG_CK(cudaEventCreate(&ev));
     for (auto& ev : user_events) LG_CK(cudaEventCreate(&ev));

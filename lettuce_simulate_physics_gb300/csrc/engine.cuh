@@ -102,6 +102,12 @@ struct Engine {
     // Walk settings (LETTUCE_CUDA_WALK / LETTUCE_CUDA_GROUP).
     bool walk_body = false;
     int group_max = 128;
+    // Walk groups: the reference's groups (default: interaction lists and counts equal to the
+    // reference CPU backend's), or with LETTUCE_GB300_WALK_GROUPS=merged consecutive sibling groups
+    // packed into groups of up to LETTUCE_GB300_WALK_MERGE_CAP bodies (fewer, fuller groups; faster
+    // on some distributions, slower on others).
+    bool walk_merge = false;
+    int merge_cap = 128;
     DirectShape direct_shape_override{0, 0, 0};
 
     // State.

@@ -103,6 +103,9 @@ struct TreeState {
     const float* inv_theta_sys = nullptr;
     uint64_t generation = 0;  // bumped by every build that may grow (reallocate) tree buffers
     DevBuf mkeys;   // forest: Morton keys before the (system, key) sort
+    // merged walk groups
+    bool merged = false;
+    DevBuf mcount, moff, mrange, mbox;
     DevBuf sticky;  // graph mode: sticky word set when a sync-free build misses
 };
 
@@ -931,6 +934,76 @@ __global__ void k_groups(const uint32_t* grp_node, const uint2* pn_lohi, uint32_
                                      __fmul_rn(0.5f, __fsub_rn(mxz, mnz)), 0.f);
 }
 
+// ---- merged walk groups (GB300 grouping; off by default) ------------------------------------
+// The reference's groups are the largest subtrees of <= group_max bodies, which the octree's
+// eight-way split leaves small (a few dozen bodies). Runs of consecutive sibling groups (same
+// parent, contiguous bodies) are packed greedily, in order, into groups of <= group_max bodies:
+// fewer, fuller walk groups. Every packed group is still contained in its parent, whose walk
+// rule opens it, so the lists stay exact-rule lists for the larger box.
+__device__ __forceinline__ uint32_t group_parent(const uint32_t* grp_node, const uint32_t* pn_cpu,
+                                                 const uint32_t* nd_parent, uint32_t T, uint32_t g) {
+    const uint32_t v = grp_node[g];
+    if (v >= T) return 0xffffffffu;
+    const uint32_t c = pn_cpu[v];
+    return c < T ? nd_parent[c] : 0xffffffffu;
+}
+
+template <bool WRITE>
+__global__ void k_merge_groups(const uint32_t* grp_node, const uint32_t* pn_cpu, const uint32_t* nd_parent,
+                               const uint2* grp_range, const unsigned* ngroups, uint32_t Tcap, const unsigned* Tdev,
+                               int gmax, uint32_t* mcount, const uint32_t* moff, uint2* mrange) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= Tcap) return;
+    const uint32_t T = eff(Tdev, Tcap), G = min(*ngroups, Tcap);
+    if (g >= G) {
+        if (!WRITE) mcount[g] = 0;
+        return;
+    }
+    const uint32_t P = group_parent(grp_node, pn_cpu, nd_parent, T, g);
+    const bool start = g == 0 || group_parent(grp_node, pn_cpu, nd_parent, T, g - 1) != P ||
+                       grp_range[g - 1].y != grp_range[g].x;
+    if (!start) {
+        if (!WRITE) mcount[g] = 0;
+        return;
+    }
+    uint32_t bins = 0, cur = 0, lo = grp_range[g].x, hi = lo;
+    for (uint32_t h = g; h < G; ++h) {
+        const uint2 r = grp_range[h];
+        if (h > g && (group_parent(grp_node, pn_cpu, nd_parent, T, h) != P || r.x != hi)) break;
+        const uint32_t sz = r.y - r.x;
+        if (cur > 0 && cur + sz > static_cast<uint32_t>(gmax)) {
+            if (WRITE) mrange[moff[g] + bins] = make_uint2(lo, hi);
+            ++bins;
+            cur = 0;
+            lo = r.x;
+        }
+        cur += sz;
+        hi = r.y;
+    }
+    if (WRITE) mrange[moff[g] + bins] = make_uint2(lo, hi);
+    ++bins;
+    if (!WRITE) mcount[g] = bins;
+}
+
+__global__ void k_merged_boxes(const uint2* mrange, const unsigned* mcount_total, uint32_t cap, const BodyArrays b,
+                               float4* box) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= *mcount_total || g >= cap) return;
+    const uint2 r = mrange[g];
+    if (r.x >= r.y) return;
+    float4 p = b.hm[r.x];
+    float mnx = p.x, mny = p.y, mnz = p.z, mxx = mnx, mxy = mny, mxz = mnz;
+    for (uint32_t i = r.x + 1; i < r.y; ++i) {
+        p = b.hm[i];
+        mnx = fminf(mnx, p.x); mny = fminf(mny, p.y); mnz = fminf(mnz, p.z);
+        mxx = fmaxf(mxx, p.x); mxy = fmaxf(mxy, p.y); mxz = fmaxf(mxz, p.z);
+    }
+    box[2 * g] = make_float4(__fmul_rn(0.5f, __fadd_rn(mnx, mxx)), __fmul_rn(0.5f, __fadd_rn(mny, mxy)),
+                             __fmul_rn(0.5f, __fadd_rn(mnz, mxz)), 0.f);
+    box[2 * g + 1] = make_float4(__fmul_rn(0.5f, __fsub_rn(mxx, mnx)), __fmul_rn(0.5f, __fsub_rn(mxy, mny)),
+                                 __fmul_rn(0.5f, __fsub_rn(mxz, mnz)), 0.f);
+}
+
 // ---- upsweep ---------------------------------------------------------------------------------
 struct Moments {
     float4* com;    // (cx, cy, cz, m), the reference's stored floats
@@ -1465,6 +1538,27 @@ void tree_build(Engine& e, double theta) {
                                t.grp_range.as<uint2>(), t.grp_box.as<float4>());
     LG_LAUNCHED();
     e.launches += 3;
+    t.merged = e.walk_merge && !sys;
+    if (t.merged) {
+        t.mcount.reserve(T * 4 + 4);
+        t.moff.reserve(T * 4 + 4);
+        t.mrange.reserve(T * 8 + 8);
+        t.mbox.reserve(T * 32 + 32);
+        k_merge_groups<false><<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_cpu.as<uint32_t>(),
+                                                t.nd_parent.as<uint32_t>(), t.grp_range.as<uint2>(), counts + 3, Tc,
+                                                Tdev, std::min(e.merge_cap, t.group_max), t.mcount.as<uint32_t>(),
+                                                nullptr, nullptr);
+        LG_LAUNCHED();
+        scan_u32(e, t, t.mcount.as<uint32_t>(), t.moff.as<uint32_t>(), static_cast<int>(T), counts + 5);
+        k_merge_groups<true><<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_cpu.as<uint32_t>(),
+                                               t.nd_parent.as<uint32_t>(), t.grp_range.as<uint2>(), counts + 3, Tc,
+                                               Tdev, std::min(e.merge_cap, t.group_max), nullptr,
+                                               t.moff.as<uint32_t>(), t.mrange.as<uint2>());
+        LG_LAUNCHED();
+        k_merged_boxes<<<tb, BS, 0, s>>>(t.mrange.as<uint2>(), counts + 5, Tc, e.bodies(e.cur), t.mbox.as<float4>());
+        LG_LAUNCHED();
+        e.launches += 3;
+    }
     // Upsweep: leaves (by size), then internal nodes level by level from the deepest.
     t.ups.reserve(sizeof(UpsweepIndex));
     t.dep_nodes.reserve(T * 4);
@@ -1561,9 +1655,9 @@ TreeView tree_view(Engine& e) {
     v.nd_comlo = t.nd_comlo.as<float4>();
     v.nd_q0 = t.nd_q0.as<float4>();
     v.nd_q1 = t.nd_q1.as<float4>();
-    v.grp_range = t.grp_range.as<uint2>();
-    v.grp_box = t.grp_box.as<float4>();
-    v.ngroups = t.counts.as<unsigned>() + 3;
+    v.grp_range = t.merged ? t.mrange.as<uint2>() : t.grp_range.as<uint2>();
+    v.grp_box = t.merged ? t.mbox.as<float4>() : t.grp_box.as<float4>();
+    v.ngroups = t.counts.as<unsigned>() + (t.merged ? 5 : 3);
     v.T = t.T;  // capacity the build was launched with (>= the node count)
     v.nd_parent = t.nd_parent.as<uint32_t>();
     v.body_leaf = t.leafid.as<uint32_t>();
@@ -1581,7 +1675,7 @@ void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* 
     LG_CK(cudaStreamSynchronize(e.stream));
     if (nodes) *nodes = e.pinned_small[2];
     if (leaves) *leaves = e.pinned_small[1];
-    if (groups) *groups = e.pinned_small[3];
+    if (groups) *groups = e.pinned_small[t.merged ? 5 : 3];
     if (max_depth) *max_depth = static_cast<int>(e.pinned_small[4]);
 }
 
@@ -1639,10 +1733,13 @@ void tree_groups(Engine& e, float* box6, uint32_t* lohi, size_t groups) {
     size_t G = 0;
     tree_counts(e, nullptr, nullptr, &G, nullptr);
     if (groups < G) fail(kArg, "tree_groups: output holds fewer than the group count");
-    if (lohi) LG_CK(cudaMemcpyAsync(lohi, t.grp_range.as<uint2>(), G * 8, cudaMemcpyDeviceToHost, e.stream));
+    // The walk's groups (merged ones when the engine packs them).
+    const uint2* range = t.merged ? t.mrange.as<uint2>() : t.grp_range.as<uint2>();
+    const float4* gbox = t.merged ? t.mbox.as<float4>() : t.grp_box.as<float4>();
+    if (lohi) LG_CK(cudaMemcpyAsync(lohi, range, G * 8, cudaMemcpyDeviceToHost, e.stream));
     if (box6) {
         std::vector<float4> box(2 * G);
-        LG_CK(cudaMemcpyAsync(box.data(), t.grp_box.as<float4>(), G * 32, cudaMemcpyDeviceToHost, e.stream));
+        LG_CK(cudaMemcpyAsync(box.data(), gbox, G * 32, cudaMemcpyDeviceToHost, e.stream));
         LG_CK(cudaStreamSynchronize(e.stream));
         for (size_t g = 0; g < G; ++g) {
             box6[6 * g] = box[2 * g].x; box6[6 * g + 1] = box[2 * g].y; box6[6 * g + 2] = box[2 * g].z;

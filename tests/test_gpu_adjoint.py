@@ -117,8 +117,19 @@ def test_tree_adjoint_theta0_equals_direct_adjoint(be):
     assert _rel(gxt, gxd) <= 1e-5 and _rel(gvt, gvd) <= 1e-5 and _rel(gmt, gmd) <= 1e-5
 
 
-@pytest.mark.parametrize("theta", [0.6, 0.3])
-def test_tree_adjoint_vs_frozen_list_central_differences(be, theta):
+def _engine_with_groups(mode):
+    import os
+    old = os.environ.get("LETTUCE_GB300_WALK_GROUPS")
+    os.environ["LETTUCE_GB300_WALK_GROUPS"] = mode
+    try:
+        return L.CudaBackend(0)
+    finally:
+        os.environ["LETTUCE_GB300_WALK_GROUPS"] = old if old is not None else "reference"
+
+
+@pytest.mark.parametrize("theta,groups", [(0.6, "reference"), (0.3, "reference"), (0.6, "merged")])
+def test_tree_adjoint_vs_frozen_list_central_differences(be, theta, groups):
+    be = _engine_with_groups(groups)
     b = S.plummer(3000, 4, cut=10)
     n = len(b)
     G, eps, dt, steps, every = 1.0, 0.02, 2e-3, 6, 2
@@ -171,9 +182,10 @@ def test_tree_adjoint_vs_frozen_list_central_differences(be, theta):
     fd = (fz.loss(x0 + hh * dx, v0 + hh * dv, m + hh * dm, G, eps, dt, xstar)
           - fz.loss(x0 - hh * dx, v0 - hh * dv, m - hh * dm, G, eps, dt, xstar)) / (2 * hh)
     ad = float((gx * dx).sum() + (gv * dv).sum() + (gm * dm).sum())
-    print(f"theta={theta}: directional {ad:.9e} vs FD {fd:.9e}; worst sampled {worst:.2e}")
+    print(f"theta={theta} {groups}: directional {ad:.9e} vs FD {fd:.9e}; worst sampled {worst:.2e}")
     assert abs(ad - fd) <= 1e-4 * abs(fd), (ad, fd)
     fz.close()
+    be.close()
 
 
 @pytest.mark.parametrize("method", [L.ForceMethod.direct, L.ForceMethod.tree])
