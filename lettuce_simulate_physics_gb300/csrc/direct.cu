@@ -48,7 +48,7 @@ template <int IPT, bool POT, bool EPS0>
 __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __restrict__ hm,
                                              const float4* __restrict__ lo, int base, int iend, int j0, int j1,
                                              float G, float e2, float4* __restrict__ out, bool write_final,
-                                             unsigned* err) {
+                                             unsigned* err, float* __restrict__ cost = nullptr) {
     const int tid = threadIdx.x;
     const int ntiles = (j1 - j0 + TILE - 1) / TILE;
     const int n = iend;
@@ -188,9 +188,10 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
             // The self pair's potential term, exactly as the loop formed it (r2 == e2).
             p = __fsub_rn(p, __fmul_rn(mself[u], rsqrt_mufu(e2)));
         }
-        if (write_final)
+        if (write_final) {
             out[i] = make_float4(G * (sx[u] - cx[u]), G * (sy[u] - cy[u]), G * (sz[u] - cz[u]), POT ? -G * p : 0.f);
-        else
+            if (cost) cost[i] = static_cast<float>(n - 1);  // interactions: every other body
+        } else
             out[i] = make_float4(sx[u] - cx[u], sy[u] - cy[u], sz[u] - cz[u], POT ? p : 0.f);
     }
 }
@@ -198,11 +199,12 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
 template <int IPT, bool POT, bool EPS0>
 __global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
                                                 int jslice, float G, float e2, float4* __restrict__ out, int write_final,
-                                                unsigned* err) {
+                                                unsigned* err, float* cost) {
     __shared__ DirectSmem sm;
     const int j0 = blockIdx.y * jslice;
     direct_block<IPT, POT, EPS0>(sm, hm, lo, blockIdx.x * (DBS * IPT), n, j0, min(n, j0 + jslice), G, e2,
-                                 write_final ? out : out + static_cast<size_t>(blockIdx.y) * n, write_final != 0, err);
+                                 write_final ? out : out + static_cast<size_t>(blockIdx.y) * n, write_final != 0, err,
+                                 cost);
 }
 
 // Many independent systems in one launch: block b takes work item b (an i-tile of one system
@@ -217,9 +219,11 @@ __global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct_batch(const floa
 }
 
 // Sums the split-j partials in slice order (Kahan) and scales by G.
-__global__ void k_direct_reduce(const float4* __restrict__ partial, int n, int slices, float G, float4* __restrict__ acc) {
+__global__ void k_direct_reduce(const float4* __restrict__ partial, int n, int slices, float G, float4* __restrict__ acc,
+                                float* __restrict__ cost) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (cost) cost[i] = static_cast<float>(n - 1);
     float s[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
     for (int k = 0; k < slices; ++k) {
         const float4 p = partial[static_cast<size_t>(k) * n + i];
@@ -233,14 +237,14 @@ __global__ void k_direct_reduce(const float4* __restrict__ partial, int n, int s
 
 template <int IPT>
 void launch_ipt(const BodyArrays b, int n, float G, float e2, bool pot, bool eps0, int jslice, int slices, float4* out,
-                int write_final, unsigned* err, cudaStream_t s) {
+                int write_final, unsigned* err, float* cost, cudaStream_t s) {
     dim3 grid((n + DBS * IPT - 1) / (DBS * IPT), slices);
     if (pot) {
-        if (eps0) k_direct<IPT, true, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
-        else k_direct<IPT, true, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+        if (eps0) k_direct<IPT, true, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        else k_direct<IPT, true, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
     } else {
-        if (eps0) k_direct<IPT, false, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
-        else k_direct<IPT, false, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err);
+        if (eps0) k_direct<IPT, false, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        else k_direct<IPT, false, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
     }
     LG_LAUNCHED();
 }
@@ -297,7 +301,7 @@ DirectShape default_direct_shape(int n, int sms) {
 }
 
 void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential, bool eps0, const DirectShape& shape,
-                   float4* acc, float4* partial, unsigned* err, cudaStream_t s) {
+                   float4* acc, float4* partial, unsigned* err, cudaStream_t s, float* cost) {
     if (n <= 0) return;
     int slices = shape.slices < 1 ? 1 : shape.slices;
     // Slices are whole 16-byte bodies of any length; tiles inside a slice may be partial.
@@ -306,13 +310,13 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
     const bool final_out = slices == 1;
     float4* out = final_out ? acc : partial;
     switch (shape.ipt) {
-        case 1: launch_ipt<1>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
-        case 2: launch_ipt<2>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
-        case 8: launch_ipt<8>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
-        default: launch_ipt<4>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, s); break;
+        case 1: launch_ipt<1>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
+        case 2: launch_ipt<2>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
+        case 8: launch_ipt<8>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
+        default: launch_ipt<4>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
     }
     if (!final_out) {
-        k_direct_reduce<<<(n + 255) / 256, 256, 0, s>>>(partial, n, slices, G, acc);
+        k_direct_reduce<<<(n + 255) / 256, 256, 0, s>>>(partial, n, slices, G, acc, cost);
         LG_LAUNCHED();
     }
 }

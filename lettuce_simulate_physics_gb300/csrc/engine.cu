@@ -277,10 +277,9 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, const
         DirectShape sh = direct_shape_override.ipt ? direct_shape_override : default_direct_shape(n, sms);
         int slices = std::max(1, sh.slices);
         if (slices > 1) partial.reserve(static_cast<size_t>(slices) * n * 16 + 16 * 1024);
-        launch_direct(b, n, G, e2, potential, eps0, sh, acc.as<float4>(), partial.as<float4>(), err_word(), stream);
+        launch_direct(b, n, G, e2, potential, eps0, sh, acc.as<float4>(), partial.as<float4>(), err_word(), stream,
+                      b.cost);
         launches += slices > 1 ? 2 : 1;
-        launch_fill_cost(b.cost, static_cast<float>(n - 1), n, stream);
-        ++launches;
         // Remote trees per block of 128 consecutive bodies (src/cpu_backend.cpp:695-717).
         if (have_let) tree_walk_remote_blocks(*this, G, e2, potential, eps0, let, let_body_blocks(*this, 128));
     } else {

@@ -63,8 +63,9 @@ void launch_flush(float* buf, size_t count, cudaStream_t s);
 // direct.cu
 // Accelerations (G-scaled) and potential of every body from all bodies; partial: slices * n float4
 // of scratch when shape.slices > 1.
+// cost (optional): per-body interaction counts n - 1, written by the same launches.
 void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential, bool eps0, const DirectShape& shape,
-                   float4* acc, float4* partial, unsigned* err, cudaStream_t s);
+                   float4* acc, float4* partial, unsigned* err, cudaStream_t s, float* cost = nullptr);
 DirectShape default_direct_shape(int n, int sms);
 // Batched direct sums over independent systems: one block per work item, i-bodies [base, iend)
 // (at most direct_block_bodies(ipt) of them) against j-bodies [j0, j1) of the same system, with
