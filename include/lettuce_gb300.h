@@ -177,6 +177,17 @@ typedef struct {
  * plain device buffer copied to rgb. */
 lg_status lg_render(lg_engine* e, const lg_render_options* o, unsigned char* rgb, double* extent_used);
 
+/* Block (hierarchical) time steps (no reference counterpart; the reference lists them as not done
+ * yet, docs/design.md:70-71). `steps` steps of size dt, each made of 2^max_level substeps: a body
+ * on level k advances with dt / 2^k in kick-drift-kick form (opening half kick where its step
+ * starts, every body drifts each substep in FP64, forces and the closing half kick where its step
+ * ends; tree walks skip the groups with no body ending a step). Levels: dt_i = eta sqrt(eps / |a_i|),
+ * k_i = the smallest k with dt / 2^k <= dt_i, clamped to [0, max_level] and, when changed, to the
+ * levels whose step starts at that time. The first call after an upload evaluates every force and
+ * level. lg_block_levels reads the levels in download order. */
+lg_status lg_block_step(lg_engine* e, const lg_force_params* p, double dt, int max_level, double eta, int steps);
+lg_status lg_block_levels(lg_engine* e, uint8_t* levels, size_t n);
+
 /* FP64-preserving restart (no reference counterpart). lg_upload64 is lg_upload with FP64 positions.
  * A float snapshot (the reference's .snap, src/snapshot.hpp:1-27) loses the FP64 state; the sidecar
  * written next to it by lg_write_fp64_sidecar holds, in download order, the ids and the low parts

@@ -191,6 +191,8 @@ def _lib() -> C.CDLL:
         "lg_export_let_read": (st, [vp, C.c_void_p, _f, _f, _f, _f]),
         "lg_upload64": (st, [vp, C.c_size_t, _d, _d, _d, _f, _f, _f, _f, _u]),
         "lg_render": (st, [vp, C.POINTER(_CRenderOptions), C.POINTER(C.c_ubyte), _d]),
+        "lg_block_step": (st, [vp, C.POINTER(_CForceParams), C.c_double, C.c_int, C.c_double, C.c_int]),
+        "lg_block_levels": (st, [vp, C.POINTER(C.c_uint8), C.c_size_t]),
         "lg_write_fp64_sidecar": (st, [vp, C.c_char_p, C.c_uint64]),
         "lg_read_fp64_sidecar": (st, [C.c_char_p, C.c_size_t, _u, _f, _f, _f, _d, _d, _d, C.POINTER(C.c_uint64)]),
         "lg_memory_need": (st, [C.c_uint64, C.c_int, C.POINTER(_CMem)]),
@@ -334,6 +336,17 @@ class CudaBackend:
         ext = C.c_double()
         _check(self._lib.lg_render(self._h, C.byref(o), rgb.ctypes.data_as(C.POINTER(C.c_ubyte)), C.byref(ext)))
         return rgb, float(ext.value)
+
+    def block_step(self, p: ForceParams, dt: float, max_level: int, eta: float, steps: int = 1) -> None:
+        """Block (hierarchical) time steps: `steps` steps of dt, bodies on levels dt / 2^k."""
+        cp = _cparams(p)
+        _check(self._lib.lg_block_step(self._h, C.byref(cp), float(dt), int(max_level), float(eta), int(steps)))
+
+    def block_levels(self) -> np.ndarray:
+        n = self.size()
+        lv = np.zeros(max(n, 1), np.uint8)
+        _check(self._lib.lg_block_levels(self._h, lv.ctypes.data_as(C.POINTER(C.c_uint8)), n))
+        return lv[:n]
 
     def write_fp64_sidecar(self, path: str, step: int = 0) -> None:
         """The low parts of the FP64 positions, in download order, next to a float snapshot."""

@@ -102,7 +102,7 @@ BodyArrays Engine::bodies(int which) const {
     b.x = s.x.as<double>(); b.y = s.y.as<double>(); b.z = s.z.as<double>();
     b.hm = s.hm.as<float4>(); b.lo = s.lo.as<float4>();
     b.vx = s.vx.as<float>(); b.vy = s.vy.as<float>(); b.vz = s.vz.as<float>(); b.m = s.m.as<float>();
-    b.cost = s.cost.as<float>(); b.id = s.id.as<uint32_t>();
+    b.cost = s.cost.as<float>(); b.id = s.id.as<uint32_t>(); b.level = s.level.as<uint8_t>();
     return b;
 }
 
@@ -111,7 +111,7 @@ void Engine::reserve_bodies(size_t count) {
         s.x.reserve(count * 8); s.y.reserve(count * 8); s.z.reserve(count * 8);
         s.hm.reserve(count * 16); s.lo.reserve(count * 16);
         s.vx.reserve(count * 4); s.vy.reserve(count * 4); s.vz.reserve(count * 4); s.m.reserve(count * 4);
-        s.cost.reserve(count * 4); s.id.reserve(count * 4);
+        s.cost.reserve(count * 4); s.id.reserve(count * 4); s.level.reserve(count + 16);
     }
     acc.reserve(count * 16);
     staging.reserve(count * 4 * 4);
@@ -130,6 +130,7 @@ void Engine::upload(size_t count, const float* x, const float* y, const float* z
     tree_ok = false;
     costs_ok = false;
     kick_rec = drift_rec = false;
+    block_ready = false;
     times = lg_phase_times{};
     tree_reset_guess(*this);
     if (n == 0) return;
@@ -712,6 +713,25 @@ lg_status lg_export_let_read(lg_engine* e, lg_let_node* nodes, float* bx, float*
         Engine& E = eng(e);
         LG_CK(cudaSetDevice(E.dev));
         lg::let_export_read(E, nodes, bx, by, bz, bm);
+    });
+}
+
+lg_status lg_block_step(lg_engine* e, const lg_force_params* p, double dt, int max_level, double eta, int steps) {
+    return guard([&] {
+        need(p, "params");
+        eng(e).block_step(*p, dt, max_level, eta, steps);
+    });
+}
+
+lg_status lg_block_levels(lg_engine* e, uint8_t* levels, size_t n) {
+    return guard([&] {
+        Engine& E = eng(e);
+        LG_CK(cudaSetDevice(E.dev));
+        if (n < static_cast<size_t>(E.n)) lg::fail(lg::kArg, "block_levels: output holds fewer than n values");
+        if (!E.block_ready) lg::fail(lg::kLogic, "block_levels: no block step since the last upload");
+        if (E.n == 0) return;
+        LG_CK(cudaMemcpyAsync(levels, E.bodies(E.cur).level, static_cast<size_t>(E.n), cudaMemcpyDeviceToHost, E.stream));
+        LG_CK(cudaStreamSynchronize(E.stream));
     });
 }
 

@@ -51,7 +51,7 @@ struct LetView {
 };
 
 struct BodySet {
-    DevBuf x, y, z, hm, lo, vx, vy, vz, m, cost, id;
+    DevBuf x, y, z, hm, lo, vx, vy, vz, m, cost, id, level;
 };
 
 struct Engine {
@@ -76,6 +76,8 @@ struct Engine {
     void read_accel(float* ax, float* ay, float* az, float* pot);
     void read_pos64(double* x, double* y, double* z);
     void flush_l2();
+    // Block (hierarchical) time steps, block.cu.
+    void block_step(const lg_force_params& p, double dt, int max_level, double eta, int steps);
     size_t held_bytes() const;
 
     BodyArrays bodies(int which) const;
@@ -109,6 +111,9 @@ struct Engine {
     bool walk_merge = false;
     int merge_cap = 128;
     DirectShape direct_shape_override{0, 0, 0};
+    // Block time steps: the walk skips passes whose bodies all have levels below walk_kmin (< 0: off).
+    int walk_kmin = -1;
+    bool block_ready = false;
 
     // State.
     int n = 0;

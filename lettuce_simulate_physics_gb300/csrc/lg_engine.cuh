@@ -28,6 +28,7 @@ struct BodyArrays {
     float4 *hm = nullptr, *lo = nullptr;
     float *vx = nullptr, *vy = nullptr, *vz = nullptr, *m = nullptr, *cost = nullptr;
     uint32_t* id = nullptr;
+    uint8_t* level = nullptr;  // block time-step level (dt = dt_base / 2^level)
 };
 
 // Direct-sum launch shape, chosen by the host (autotuned or defaults).

@@ -483,6 +483,7 @@ __global__ void k_permute(const BodyArrays src, BodyArrays dst, const uint64_t* 
         dst.hm[i] = src.hm[i]; dst.lo[i] = src.lo[i];
         dst.vx[i] = src.vx[i]; dst.vy[i] = src.vy[i]; dst.vz[i] = src.vz[i];
         dst.m[i] = src.m[i]; dst.id[i] = src.id[i]; dst.cost[i] = src.cost[i];
+        dst.level[i] = src.level[i];
         return;
     }
     if (key1_in) key1_out[i] = key1_in[j];
@@ -497,6 +498,7 @@ __global__ void k_permute(const BodyArrays src, BodyArrays dst, const uint64_t* 
     dst.m[i] = src.m[j];
     dst.id[i] = src.id[j];
     dst.cost[i] = src.cost[j];
+    dst.level[i] = src.level[j];
 }
 
 // After the passes: if the sorted pairs ended in buffer B, copy them to A (so every sort returns

@@ -76,6 +76,9 @@ struct WalkArgs {
     LetView let;
     int local;
     int accumulate;
+    // Block time steps: passes whose bodies all have level < kmin are skipped (level == nullptr: none).
+    const uint8_t* level;
+    int kmin;
 };
 
 __device__ __forceinline__ f2x ld2(const float* p) { return *reinterpret_cast<const f2x*>(p); }
@@ -275,6 +278,11 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
 template <bool POT, bool EPS0>
 __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int lane, uint2 gr, float4 bc, float4 bh,
                           uint32_t plo, int np, unsigned long long& inter_b, unsigned long long& inter_c) {
+    if (w.level) {
+        bool active = false;
+        for (int k = lane; k < np; k += 32) active |= w.level[plo + k] >= w.kmin;
+        if (!__any_sync(0xffffffffu, active)) return;
+    }
     const float ox = bc.x, oy = bc.y, oz = bc.z;
     const int ipt = (np + 31) >> 5;
     float xi[IPT_MAX], yi[IPT_MAX], zi[IPT_MAX], mi[IPT_MAX];
@@ -414,6 +422,10 @@ void tree_walk(Engine& e, float G, float e2, bool potential, bool eps0, const ui
     if (let) w.let = *let;
     w.local = 1;
     w.accumulate = 0;
+    if (e.walk_kmin >= 0) {
+        w.level = e.bodies(e.cur).level;
+        w.kmin = e.walk_kmin;
+    }
     w.tv = tree_view(e);
     BodyArrays b = e.bodies(e.cur);
     w.hm = b.hm;

@@ -1205,3 +1205,66 @@ void or_frozen_accel(const or_frozen* f, int s, const double* x, const double* m
     frozen_accel(f, s, x, m, G, eps * eps, a, mom, nt);
     free(mom);
 }
+
+/* ---- FP64 block (hierarchical) time steps, direct forces ----------------------------------------
+ * Test oracle of the engine's block steps (no reference counterpart): `steps` steps of dt, each of
+ * 2^K substeps. At substep boundary s, bodies whose level k has s a multiple of 2^(K-k) get the
+ * opening half kick dt/2^k/2; every body drifts by dt/2^K; at boundary s+1 the bodies ending a
+ * step get fresh forces, the closing half kick and a new level: the smallest k with
+ * dt/2^k <= eta sqrt(eps/|a|), i.e. k = ceil(log2((dt/eta) sqrt(|a|/eps))) by frexp, clamped to
+ * [kmin, K] with kmin = K - trailing zeros of s+1 (0 at the end of the step). Positions, velocities
+ * and accelerations in FP64; x, v (3 per body) are updated in place, levels written to level. */
+static int or_level_for(const double* a, double dt, double eta, double eps, int kmin, int kmax) {
+    const double am = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (!(am > 0)) return kmin;
+    const double r = dt / eta * sqrt(am / eps);
+    if (!(r > 1)) return kmin;
+    int e = 0;
+    const double f = frexp(r, &e);
+    int k = f == 0.5 ? e - 1 : e;
+    return k < kmin ? kmin : (k > kmax ? kmax : k);
+}
+
+static int or_tz(unsigned v) {
+    int t = 0;
+    while (v && !(v & 1u)) { v >>= 1; ++t; }
+    return t;
+}
+
+void or_block_direct_fp64(size_t n, double* x, double* v, const double* m, double G, double eps, double dt, int K,
+                          double eta, int steps, uint8_t* level, int threads) {
+    const int nt = threads > 0 ? threads : omp_get_max_threads();
+    const long ln = (long)n;
+    const double e2 = eps * eps, epsl = eps > 0 ? eps : 1e-30;
+    double* a = malloc(n * 3 * sizeof(double));
+    if (!a) abort();
+    accel_fp64(ln, x, m, G, e2, a, nt);
+    for (long i = 0; i < ln; ++i) level[i] = (uint8_t)or_level_for(a + 3 * i, dt, eta, epsl, 0, K);
+    const unsigned sub = 1u << K;
+    const double ds = ldexp(dt, -K);
+    for (int st = 0; st < steps; ++st) {
+        for (unsigned s = 0; s < sub; ++s) {
+            const int kopen = s == 0 ? 0 : K - or_tz(s);
+            for (long i = 0; i < ln; ++i)
+                if (level[i] >= kopen) {
+                    const double h = 0.5 * ldexp(dt, -level[i]);
+                    for (int c = 0; c < 3; ++c) v[3 * i + c] += h * a[3 * i + c];
+                }
+            for (long k = 0; k < 3 * ln; ++k) x[k] += ds * v[k];
+            const unsigned s1 = s + 1;
+            const int kclose = s1 == sub ? 0 : K - or_tz(s1);
+            double* an = malloc(n * 3 * sizeof(double));
+            if (!an) abort();
+            accel_fp64(ln, x, m, G, e2, an, nt);
+            for (long i = 0; i < ln; ++i)
+                if (level[i] >= kclose) {
+                    for (int c = 0; c < 3; ++c) a[3 * i + c] = an[3 * i + c];
+                    const double h = 0.5 * ldexp(dt, -level[i]);
+                    for (int c = 0; c < 3; ++c) v[3 * i + c] += h * a[3 * i + c];
+                    level[i] = (uint8_t)or_level_for(a + 3 * i, dt, eta, epsl, kclose, K);
+                }
+            free(an);
+        }
+    }
+    free(a);
+}

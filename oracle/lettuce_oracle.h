@@ -105,6 +105,11 @@ double or_frozen_loss(const or_frozen* f, const double* x0, const double* v0, co
 void or_frozen_accel(const or_frozen* f, int s, const double* x, const double* m, double G, double eps, double* a,
                      int threads);
 
+/* FP64 block (hierarchical) time steps with direct forces (test oracle of the engine's block steps):
+ * x, v (3 per body, FP64) advanced in place; level (per body) = the final levels. */
+void or_block_direct_fp64(size_t n, double* x, double* v, const double* m, double G, double eps, double dt, int K,
+                          double eta, int steps, uint8_t* level, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,9 @@ def _lib(kind: str) -> C.CDLL:
         lib.or_frozen_destroy.argtypes = [vp]
         lib.or_frozen_loss.restype = C.c_double
         lib.or_frozen_loss.argtypes = [vp, _d, _d, _d, C.c_double, C.c_double, C.c_double, _d, C.c_int]
+        lib.or_block_direct_fp64.restype = None
+        lib.or_block_direct_fp64.argtypes = [C.c_size_t, _d, _d, _d, C.c_double, C.c_double, C.c_double, C.c_int,
+                                             C.c_double, C.c_int, C.POINTER(C.c_uint8), C.c_int]
         lib.or_frozen_accel.restype = None
         lib.or_frozen_accel.argtypes = [vp, C.c_int, _d, _d, C.c_double, C.c_double, _d, C.c_int]
     _libs[kind] = lib
@@ -302,6 +305,18 @@ def loss_direct_fp64(x0, v0, m, G, eps, dt, steps, xstar, threads=0):
     xstar = np.ascontiguousarray(xstar, np.float64)
     return lib.or_loss_direct_fp64(m.shape[0], _dp(x0), _dp(v0), _dp(m), float(G), float(eps), float(dt),
                                    int(steps), _dp(xstar), int(threads))
+
+
+def block_direct_fp64(x0, v0, m, G, eps, dt, K, eta, steps, threads=0):
+    """FP64 block time steps with direct forces: (x (n, 3), v (n, 3), levels (n,))."""
+    lib = _lib("port")
+    x = np.ascontiguousarray(x0, np.float64).copy()
+    v = np.ascontiguousarray(v0, np.float64).copy()
+    m = np.ascontiguousarray(m, np.float64)
+    lv = np.zeros(len(m), np.uint8)
+    lib.or_block_direct_fp64(len(m), _dp(x), _dp(v), _dp(m), float(G), float(eps), float(dt), int(K), float(eta),
+                             int(steps), lv.ctypes.data_as(C.POINTER(C.c_uint8)), int(threads))
+    return x, v, lv
 
 
 def render_ref(b, width, height, view="xy", extent=0.0, color=0):

@@ -207,3 +207,14 @@ def test_frozen_lists_at_theta0_are_the_direct_sum():
     L2 = O.loss_direct_fp64(x0, v0, b.m, 1.0, eps, dt, steps, xs)
     assert abs(L1 - L2) <= 1e-12 * abs(L2)
     fz.close()
+
+
+def test_block_oracle_at_level_zero_is_the_plain_leapfrog():
+    """With max_level 0 the block scheme is the plain KDK leapfrog: same FP64 trajectory."""
+    b = S.plummer(400, 5, cut=20)
+    x0, v0, m = b.pos64(), b.vel64(), b.m.astype(np.float64)
+    x, v, lv = O.block_direct_fp64(x0, v0, m, 1.0, 0.02, 1e-3, 0, 0.05, 4)
+    assert not lv.any()
+    L1 = float((m[:, None] * x * x).sum())
+    L2 = O.loss_direct_fp64(x0, v0, m, 1.0, 0.02, 1e-3, 4, np.zeros_like(x0))
+    assert abs(L1 / L2 - 1) <= 1e-14  # the same trajectory; the two sums add in different orders
