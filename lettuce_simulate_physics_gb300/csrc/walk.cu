@@ -114,7 +114,7 @@ __device__ __forceinline__ f2x pair_rsqrt(f2x r2) {
 // Quadrupole cell terms: d points from the body to the cell,
 // a = G [M d/r^3 - Q d/r^5 + 5/2 (dQd) d/r^7], phi = -G [M/r + 1/2 dQd/r^5]. cc is even.
 template <int IPT, bool POT, bool EPS0>
-__device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int lane, const float (&xi)[IPT_MAX],
+__device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int k0, int kstep, int lane, const float (&xi)[IPT_MAX],
                                            const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
     f2x XI[IPT], YI[IPT], ZI[IPT], ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
@@ -127,7 +127,7 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int lane, const 
     const f2x E2 = f2_bcast(e2), C25 = f2_bcast(2.5f), NEG1 = f2_bcast(-1.f), C05 = f2_bcast(0.5f);
     // Few i-bodies per lane leave little independent work per entry: unroll over entries then.
 #pragma unroll CUNROLL
-    for (int k = 0; k < cc; k += 2) {
+    for (int k = k0; k < cc; k += kstep) {
         const f2x X = ld2(s.cx + k), Y = ld2(s.cy + k), Z = ld2(s.cz + k), M = ld2(s.cm + k);
         const f2x QXX = ld2(s.qxx + k), QXY = ld2(s.qxy + k), QXZ = ld2(s.qxz + k);
         const f2x QYY = ld2(s.qyy + k), QYZ = ld2(s.qyz + k), QZZ = ld2(s.qzz + k);
@@ -156,8 +156,9 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int lane, const 
 
 // Softened body terms a = G m d / r^3, phi = -G m / r. bc is even.
 template <int IPT, bool POT, bool EPS0>
-__device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int lane, const float (&xi)[IPT_MAX],
-                                            const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+__device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int k0, int kstep, int lane,
+                                            const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
+                                            const float (&zi)[IPT_MAX], float e2) {
     f2x XI[IPT], YI[IPT], ZI[IPT], ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
@@ -168,7 +169,7 @@ __device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int lane, const
     }
     const f2x E2 = f2_bcast(e2);
 #pragma unroll BUNROLL
-    for (int k = 0; k < bc; k += 2) {
+    for (int k = k0; k < bc; k += kstep) {
         const f2x X = ld2(s.bx + k), Y = ld2(s.by + k), Z = ld2(s.bz + k), M = ld2(s.bm + k);
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
@@ -188,24 +189,26 @@ __device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int lane, const
 }
 
 template <bool POT, bool EPS0>
-__device__ __forceinline__ void eval_cells_n(int ipt, WarpSmem& s, int cc, int lane, const float (&xi)[IPT_MAX],
-                                             const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+__device__ __forceinline__ void eval_cells_n(int ipt, WarpSmem& s, int cc, int k0, int kstep, int lane,
+                                             const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
+                                             const float (&zi)[IPT_MAX], float e2) {
     switch (ipt) {
-        case 1: eval_cells<1, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
-        case 2: eval_cells<2, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
-        case 3: eval_cells<3, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
-        default: eval_cells<4, POT, EPS0>(s, cc, lane, xi, yi, zi, e2); break;
+        case 1: eval_cells<1, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 2: eval_cells<2, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 3: eval_cells<3, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        default: eval_cells<4, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
     }
 }
 
 template <bool POT, bool EPS0>
-__device__ __forceinline__ void eval_bodies_n(int ipt, WarpSmem& s, int bc, int lane, const float (&xi)[IPT_MAX],
-                                              const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+__device__ __forceinline__ void eval_bodies_n(int ipt, WarpSmem& s, int bc, int k0, int kstep, int lane,
+                                              const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
+                                              const float (&zi)[IPT_MAX], float e2) {
     switch (ipt) {
-        case 1: eval_bodies<1, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
-        case 2: eval_bodies<2, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
-        case 3: eval_bodies<3, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
-        default: eval_bodies<4, POT, EPS0>(s, bc, lane, xi, yi, zi, e2); break;
+        case 1: eval_bodies<1, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 2: eval_bodies<2, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 3: eval_bodies<3, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
+        default: eval_bodies<4, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
     }
 }
 
@@ -214,12 +217,13 @@ constexpr float kFar = 1e18f;
 
 // Evaluates the pending lists for the pass's i-bodies and empties them.
 template <bool POT, bool EPS0>
-__device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int ipt, int nc, int nr, float ox,
-                                      float oy, float oz, const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
-                                      const float (&zi)[IPT_MAX], float e2) {
+__device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int ipt, int part, int P, int nc,
+                                      int nr, float ox, float oy, float oz, const float (&xi)[IPT_MAX],
+                                      const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+    const int pad = 2 * P - 1;  // chunks padded to whole pairs per partition
     for (int c0 = 0; c0 < nc; c0 += CCH) {
         const int cc = min(CCH, nc - c0);
-        const int cc2 = (cc + 1) & ~1;
+        const int cc2 = (cc + pad) & ~pad;
         for (int k = lane; k < cc2; k += 32) {
             if (k < cc) {
                 const uint32_t nd = s.clist[c0 + k];
@@ -242,14 +246,14 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
             }
         }
         __syncwarp();
-        eval_cells_n<POT, EPS0>(ipt, s, cc2, lane, xi, yi, zi, e2);
+        eval_cells_n<POT, EPS0>(ipt, s, cc2, 2 * part, 2 * P, lane, xi, yi, zi, e2);
         __syncwarp();
     }
     if (nr == 0) return;
     const int total = range_prefix(s, nr, lane);
     for (int b0 = 0; b0 < total; b0 += BCH) {
         const int bc = min(BCH, total - b0);
-        const int bc2 = (bc + 1) & ~1;
+        const int bc2 = (bc + pad) & ~pad;
         for (int k = lane; k < bc2; k += 32) {
             if (k < bc) {
                 const uint32_t j = range_body(s, nr, b0 + k);
@@ -270,7 +274,7 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
             }
         }
         __syncwarp();
-        eval_bodies_n<POT, EPS0>(ipt, s, bc2, lane, xi, yi, zi, e2);
+        eval_bodies_n<POT, EPS0>(ipt, s, bc2, 2 * part, 2 * P, lane, xi, yi, zi, e2);
         __syncwarp();
     }
 }
@@ -284,11 +288,23 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         if (!__any_sync(0xffffffffu, active)) return;
     }
     const float ox = bc.x, oy = bc.y, oz = bc.z;
-    const int ipt = (np + 31) >> 5;
+    // Entry partitions: the warp's lanes form P partitions of Lw = 32 / P lanes; every partition
+    // holds all np i-bodies (ipt per lane) and evaluates every P-th pair of list entries, and the
+    // partitions' sums are added at the end. P is the one of 1, 2, 4 with the least lane work
+    // ipt / P (ties to the smaller P), so small groups keep every lane busy.
+    int P = 1, ipt = (np + 31) >> 5;
+    for (int q = 2; q <= 4; q *= 2) {
+        const int iq = (np * q + 31) >> 5;
+        if (iq <= IPT_MAX && iq * P < ipt * q) {
+            P = q;
+            ipt = iq;
+        }
+    }
+    const int Lw = 32 / P, part = lane / Lw, lp = lane % Lw;
     float xi[IPT_MAX], yi[IPT_MAX], zi[IPT_MAX], mi[IPT_MAX];
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
-        const int k = min(lane + 32 * u, np - 1);
+        const int k = min(lp + Lw * u, np - 1);
         const float4 h = w.hm[plo + k], l = w.lo[plo + k];
         xi[u] = (h.x - ox) + l.x;
         yi[u] = (h.y - oy) + l.y;
@@ -302,7 +318,9 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     const uint32_t root = w.sys ? w.sys[gr.x] : 0u;
     const float e2 = w.e2_sys ? w.e2_sys[root] : w.e2;
     uint32_t list_len = 0, cells_len = 0;
-    auto fl = [&](int nc, int nr) { flush<POT, EPS0>(w, s, lane, ipt, nc, nr, ox, oy, oz, xi, yi, zi, e2); };
+    auto fl = [&](int nc, int nr) {
+        flush<POT, EPS0>(w, s, lane, ipt, part, P, nc, nr, ox, oy, oz, xi, yi, zi, e2);
+    };
     if (w.local) traverse(w.tv, s, stack, lane, gr, bc, bh, root, w.err, list_len, cells_len, fl);
     for (int t = 0; t < w.let.ntrees; ++t)
         traverse_let(w.let, s, stack, lane, bc, bh, w.let.roots[t], w.err, list_len, cells_len, fl);
@@ -313,14 +331,20 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     const float self_inv = (POT && !EPS0) ? rsqrt_mufu(e2) : 0.f;
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
-        const int k = lane + 32 * u;
-        if (k >= np) continue;
-        const uint32_t i = plo + k;
         const float* ks = &s.ks[u][0][lane];
-        float p = ks[96] - ks[224];
+        float fx = ks[0] - ks[128], fy = ks[32] - ks[160], fz = ks[64] - ks[192], p = ks[96] - ks[224];
+        // The partitions' sums, in a fixed order (all lanes take part in the shuffles).
+        for (int o = Lw; o < 32; o <<= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            fz += __shfl_xor_sync(0xffffffffu, fz, o);
+            if (POT) p += __shfl_xor_sync(0xffffffffu, p, o);
+        }
+        const int k = lp + Lw * u;
+        if (part != 0 || k >= np) continue;
+        const uint32_t i = plo + k;
         if (POT && !EPS0 && w.local) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
-        const float4 a = make_float4(w.G * (ks[0] - ks[128]), w.G * (ks[32] - ks[160]), w.G * (ks[64] - ks[192]),
-                                     POT ? -w.G * p : 0.f);
+        const float4 a = make_float4(w.G * fx, w.G * fy, w.G * fz, POT ? -w.G * p : 0.f);
         if (w.accumulate) {
             const float4 o = w.acc[i];
             w.acc[i] = make_float4(o.x + a.x, o.y + a.y, o.z + a.z, o.w + a.w);
