@@ -51,8 +51,11 @@ inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) 
 // ---- sort control --------------------------------------------------------------------------
 constexpr int RADIX = 256;
 constexpr int PASSES = 8;
+#ifndef LG_SORT_IPT
+#define LG_SORT_IPT 8
+#endif
 constexpr int SORT_BS = 256;
-constexpr int SORT_IPT = 8;
+constexpr int SORT_IPT = LG_SORT_IPT;  // keys per thread of a sort tile
 constexpr int SORT_TILE = SORT_BS * SORT_IPT;
 constexpr unsigned FLAG_AGG = 1u << 30, FLAG_INC = 2u << 30, VAL_MASK = (1u << 30) - 1;
 
