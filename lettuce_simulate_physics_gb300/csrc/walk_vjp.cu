@@ -28,7 +28,7 @@
 // chunk is converted once to group-relative FP32 coordinates in shared memory and evaluated twice:
 // lanes over i-bodies for the i side (Kahan sums in shared memory), and lanes over entries, looping
 // over the group's i-bodies, for the entry side (sums per entry added to FP64 adjoint arrays with
-// atomics).
+// atomics). Both evaluate two pairs per packed f32x2 instruction.
 #include "engine.cuh"
 #include "walk_common.cuh"
 
@@ -51,6 +51,7 @@ struct __align__(16) VjpSmem {
     float bx[VBCH], by[VBCH], bz[VBCH], bm[VBCH];
     uint32_t bj[VBCH];
     float ix[VPASS], iy[VPASS], iz[VPASS], iwx[VPASS], iwy[VPASS], iwz[VPASS];
+    int kself[VPASS];  // per i-body: its position in the current body chunk, or -2
     float ks[VIPT][6][32];  // i-side Kahan sums of gd (x, y, z) and compensations
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];
@@ -79,8 +80,9 @@ __device__ __forceinline__ float inv_r(float r2) {
     return EPS0 ? (r2 > 0.f ? v : 0.f) : v;
 }
 
-__device__ __forceinline__ void kahan3(VjpSmem& s, int u, int lane, float x, float y, float z) {
-    float* k = &s.ks[u][0][lane];
+// Adds (x, y, z) to the Kahan sums of i-body i (slot lane i % 32 of pass i / 32).
+__device__ __forceinline__ void kahan3(VjpSmem& s, int i, float x, float y, float z) {
+    float* k = &s.ks[i >> 5][0][i & 31];
     float sx = k[0], sy = k[32], sz = k[64], cx = k[96], cy = k[128], cz = k[160];
     kahan_add(sx, cx, x);
     kahan_add(sy, cy, y);
@@ -88,99 +90,156 @@ __device__ __forceinline__ void kahan3(VjpSmem& s, int u, int lane, float x, flo
     k[0] = sx; k[32] = sy; k[64] = sz; k[96] = cx; k[128] = cy; k[160] = cz;
 }
 
-// Cell term: gd for weight w at offset d (cell minus body); also returns u / r^3, u / r^5 and
-// u / r^7 pieces through the out parameters the entry side needs.
-struct CellJ {
-    float gdx, gdy, gdz, u, inv3, inv5, inv7;
+// Entry partitions of the i-side loops: the warp's lanes form P groups of 32 / P lanes, each
+// holding every i-body and taking every P-th entry pair; P (1, 2 or 4) is the one with the least
+// lane work for np i-bodies (ties to the smaller P). Warp-uniform.
+__device__ __forceinline__ int vjp_parts(int np) {
+    const int w1 = 4 * ((np + 31) >> 5), w2 = 2 * ((np + 15) >> 4), w4 = (np + 7) >> 3;  // quarter sweeps
+    return w4 < w2 && w4 < w1 ? 4 : (w2 < w1 ? 2 : 1);
+}
+
+// Sum of v over the P partitions (lanes lane, lane ^ Lw, ...); every lane takes part.
+__device__ __forceinline__ float part_sum(float v, int P) {
+    if (P >= 4) v += __shfl_xor_sync(0xffffffffu, v, 8);
+    if (P >= 2) v += __shfl_xor_sync(0xffffffffu, v, 16);
+    return v;
+}
+
+// Two adjacent floats of a shared-memory array as one packed pair (k even).
+__device__ __forceinline__ f2x ld2(const float* p, int k) { return *reinterpret_cast<const f2x*>(p + k); }
+
+template <bool EPS0>
+__device__ __forceinline__ f2x inv_r2(f2x r2) {
+    float lo, hi;
+    f2_unpack(r2, lo, hi);
+    return f2_pack(inv_r<EPS0>(lo), inv_r<EPS0>(hi));
+}
+
+// Cell term for two (body, cell) pairs at once: gd for weight w at offset d (cell minus body); also
+// u = w.d, u / r^3, D = 5 u / r^7 and n5 = -1 / r^5, which the entry side reuses.
+struct CellJ2 {
+    f2x gdx, gdy, gdz, u, inv3, D, n5;
 };
 
-__device__ __forceinline__ CellJ cell_j(float dx, float dy, float dz, float inv, float M, float qxx, float qxy,
-                                        float qxz, float qyy, float qyz, float qzz, float wx, float wy, float wz) {
-    CellJ c;
-    const float inv2 = inv * inv, inv3 = inv * inv2, inv5 = inv3 * inv2, inv7 = inv5 * inv2, inv9 = inv7 * inv2;
-    const float qx = qxx * dx + qxy * dy + qxz * dz;
-    const float qy = qxy * dx + qyy * dy + qyz * dz;
-    const float qz = qxz * dx + qyz * dy + qzz * dz;
-    const float q = dx * qx + dy * qy + dz * qz;
-    const float u = wx * dx + wy * dy + wz * dz;
-    const float qwx = qxx * wx + qxy * wy + qxz * wz;
-    const float qwy = qxy * wx + qyy * wy + qyz * wz;
-    const float qwz = qxz * wx + qyz * wy + qzz * wz;
-    const float wqd = wx * qx + wy * qy + wz * qz;
-    const float A = M * inv3 + 2.5f * q * inv7;
-    const float B = -3.f * M * u * inv5 + 5.f * wqd * inv7 - 17.5f * q * u * inv9;
-    const float D = 5.f * u * inv7;
-    c.gdx = A * wx + B * dx - qwx * inv5 + D * qx;
-    c.gdy = A * wy + B * dy - qwy * inv5 + D * qy;
-    c.gdz = A * wz + B * dz - qwz * inv5 + D * qz;
+__device__ __forceinline__ CellJ2 cell_j2(f2x dx, f2x dy, f2x dz, f2x inv, f2x M, f2x qxx, f2x qxy, f2x qxz, f2x qyy,
+                                          f2x qyz, f2x qzz, f2x wx, f2x wy, f2x wz) {
+    const f2x C25 = f2_bcast(2.5f), C5 = f2_bcast(5.f), CN3 = f2_bcast(-3.f), CN175 = f2_bcast(-17.5f);
+    const f2x CN1 = f2_bcast(-1.f);
+    CellJ2 c;
+    const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv, inv2), inv5 = f2_mul(inv3, inv2);
+    const f2x inv7 = f2_mul(inv5, inv2), inv9 = f2_mul(inv7, inv2);
+    const f2x qx = f2_fma(qxx, dx, f2_fma(qxy, dy, f2_mul(qxz, dz)));
+    const f2x qy = f2_fma(qxy, dx, f2_fma(qyy, dy, f2_mul(qyz, dz)));
+    const f2x qz = f2_fma(qxz, dx, f2_fma(qyz, dy, f2_mul(qzz, dz)));
+    const f2x q = f2_fma(dx, qx, f2_fma(dy, qy, f2_mul(dz, qz)));
+    const f2x u = f2_fma(wx, dx, f2_fma(wy, dy, f2_mul(wz, dz)));
+    const f2x qwx = f2_fma(qxx, wx, f2_fma(qxy, wy, f2_mul(qxz, wz)));
+    const f2x qwy = f2_fma(qxy, wx, f2_fma(qyy, wy, f2_mul(qyz, wz)));
+    const f2x qwz = f2_fma(qxz, wx, f2_fma(qyz, wy, f2_mul(qzz, wz)));
+    const f2x wqd = f2_fma(wx, qx, f2_fma(wy, qy, f2_mul(wz, qz)));
+    // A = M / r^3 + 5/2 q / r^7;  B = -3 M u / r^5 + 5 (w.Qd) / r^7 - 35/2 q u / r^9;  D = 5 u / r^7
+    const f2x A = f2_fma(M, inv3, f2_mul(f2_mul(C25, q), inv7));
+    const f2x B = f2_fma(f2_mul(CN3, f2_mul(M, u)), inv5,
+                         f2_fma(f2_mul(C5, wqd), inv7, f2_mul(f2_mul(CN175, f2_mul(q, u)), inv9)));
+    const f2x D = f2_mul(f2_mul(C5, u), inv7);
+    const f2x n5 = f2_mul(CN1, inv5);
+    c.gdx = f2_fma(A, wx, f2_fma(B, dx, f2_fma(D, qx, f2_mul(qwx, n5))));
+    c.gdy = f2_fma(A, wy, f2_fma(B, dy, f2_fma(D, qy, f2_mul(qwy, n5))));
+    c.gdz = f2_fma(A, wz, f2_fma(B, dz, f2_fma(D, qz, f2_mul(qwz, n5))));
     c.u = u;
     c.inv3 = inv3;
-    c.inv5 = inv5;
-    c.inv7 = inv7;
+    c.D = D;
+    c.n5 = n5;
     return c;
 }
 
+// One flush of the pending list: nc cells (s.clist) and nr body ranges (s.rlist) against the
+// group's np i-bodies of this pass. Every loop evaluates two pairs per packed instruction: the
+// i-side loops (lanes over i-bodies) take the entries two at a time, the entry-side loops (lanes
+// over entries) take the i-bodies two at a time. Odd counts are padded with one zero-weight copy
+// of the last element (cells: M = Q = 0; bodies: m = 0; i-bodies: w = 0), whose terms are exactly
+// zero. The self pair (body j == body i) is removed by zeroing its half of the mass (i side) or of
+// the weight (entry side).
 template <bool EPS0>
 __device__ void vjp_flush(const VjpArgs& a, VjpSmem& s, int lane, int np, uint32_t plo, int nc, int nr, float ox,
                           float oy, float oz, float e2) {
     const size_t T = a.tv.T;
+    const f2x E2 = f2_bcast(e2), C05 = f2_bcast(0.5f), CN3 = f2_bcast(-3.f);
+    const int P = vjp_parts(np), Lw = 32 / P, part = lane / Lw, lp = lane % Lw;
+    const int nuP = (np + Lw - 1) / Lw;  // i-body rounds of the i-side loops (warp-uniform)
+    const int npe = (np + 1) & ~1;
     // ---- cells
     for (int c0 = 0; c0 < nc; c0 += VCCH) {
         const int cc = min(VCCH, nc - c0);
         for (int k = lane; k < cc; k += 32) {
             const uint32_t nd = s.clist[c0 + k];
             const float4 com = a.tv.nd_com[nd], cl = a.tv.nd_comlo[nd], q0 = a.tv.nd_q0[nd], q1 = a.tv.nd_q1[nd];
-            s.cx[k] = (com.x - ox) + cl.x;
-            s.cy[k] = (com.y - oy) + cl.y;
-            s.cz[k] = (com.z - oz) + cl.z;
+            const float X = (com.x - ox) + cl.x, Y = (com.y - oy) + cl.y, Z = (com.z - oz) + cl.z;
+            s.cx[k] = X; s.cy[k] = Y; s.cz[k] = Z;
             s.cm[k] = com.w;
             s.qxx[k] = q0.x; s.qxy[k] = q0.y; s.qxz[k] = q0.z; s.qyy[k] = q0.w; s.qyz[k] = q1.x; s.qzz[k] = q1.y;
+            if (k == cc - 1 && (cc & 1)) {
+                s.cx[cc] = X; s.cy[cc] = Y; s.cz[cc] = Z;
+                s.cm[cc] = 0.f;
+                s.qxx[cc] = 0.f; s.qxy[cc] = 0.f; s.qxz[cc] = 0.f; s.qyy[cc] = 0.f; s.qyz[cc] = 0.f; s.qzz[cc] = 0.f;
+            }
         }
         __syncwarp();
-        // i side: lanes over i-bodies.
-#pragma unroll
-        for (int u = 0; u < VIPT; ++u) {
-            const int i = lane + 32 * u;
-            if (i >= np) continue;
-            const float xi = s.ix[i], yi = s.iy[i], zi = s.iz[i], wx = s.iwx[i], wy = s.iwy[i], wz = s.iwz[i];
-            float ax = 0.f, ay = 0.f, az = 0.f;
-            for (int k = 0; k < cc; ++k) {
-                const float dx = s.cx[k] - xi, dy = s.cy[k] - yi, dz = s.cz[k] - zi;
-                const float inv = inv_r<EPS0>(dx * dx + dy * dy + dz * dz + e2);
-                const CellJ j = cell_j(dx, dy, dz, inv, s.cm[k], s.qxx[k], s.qxy[k], s.qxz[k], s.qyy[k], s.qyz[k],
-                                       s.qzz[k], wx, wy, wz);
-                ax += j.gdx;
-                ay += j.gdy;
-                az += j.gdz;
+        // i side: lanes over i-bodies, cells two at a time (every P-th pair per partition).
+        for (int u = 0; u < nuP; ++u) {
+            const int i = lp + Lw * u;
+            const f2x xi = f2_bcast(s.ix[i]), yi = f2_bcast(s.iy[i]), zi = f2_bcast(s.iz[i]);
+            const f2x wx = f2_bcast(s.iwx[i]), wy = f2_bcast(s.iwy[i]), wz = f2_bcast(s.iwz[i]);
+            f2x ax = f2_bcast(0.f), ay = ax, az = ax;
+#pragma unroll 2
+            for (int k = 2 * part; k < cc; k += 2 * P) {
+                const f2x dx = f2_sub(ld2(s.cx, k), xi), dy = f2_sub(ld2(s.cy, k), yi), dz = f2_sub(ld2(s.cz, k), zi);
+                const f2x inv = inv_r2<EPS0>(f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2))));
+                const CellJ2 j = cell_j2(dx, dy, dz, inv, ld2(s.cm, k), ld2(s.qxx, k), ld2(s.qxy, k), ld2(s.qxz, k),
+                                         ld2(s.qyy, k), ld2(s.qyz, k), ld2(s.qzz, k), wx, wy, wz);
+                ax = f2_add(ax, j.gdx);
+                ay = f2_add(ay, j.gdy);
+                az = f2_add(az, j.gdz);
             }
-            kahan3(s, u, lane, ax, ay, az);
+            const float sx = part_sum(f2_sum(ax), P), sy = part_sum(f2_sum(ay), P), sz = part_sum(f2_sum(az), P);
+            if (part == 0 && i < np) kahan3(s, i, sx, sy, sz);
         }
-        // Entry side: lanes over cells, looping over the group's i-bodies.
+        // Entry side: lanes over cells, the group's i-bodies two at a time.
         for (int k = lane; k < cc; k += 32) {
-            const float X = s.cx[k], Y = s.cy[k], Z = s.cz[k], M = s.cm[k];
-            const float qxx = s.qxx[k], qxy = s.qxy[k], qxz = s.qxz[k], qyy = s.qyy[k], qyz = s.qyz[k], qzz = s.qzz[k];
-            float g[NADJ] = {};
-            for (int i = 0; i < np; ++i) {
-                const float wx = s.iwx[i], wy = s.iwy[i], wz = s.iwz[i];
-                const float dx = X - s.ix[i], dy = Y - s.iy[i], dz = Z - s.iz[i];
-                const float inv = inv_r<EPS0>(dx * dx + dy * dy + dz * dz + e2);
-                const CellJ j = cell_j(dx, dy, dz, inv, M, qxx, qxy, qxz, qyy, qyz, qzz, wx, wy, wz);
-                const float E = 2.5f * j.u * j.inv7;
-                g[0] += j.u * j.inv3;
-                g[1] += j.gdx;
-                g[2] += j.gdy;
-                g[3] += j.gdz;
-                g[4] += E * dx * dx - wx * dx * j.inv5;
-                g[5] += 2.f * E * dx * dy - (wx * dy + wy * dx) * j.inv5;
-                g[6] += 2.f * E * dx * dz - (wx * dz + wz * dx) * j.inv5;
-                g[7] += E * dy * dy - wy * dy * j.inv5;
-                g[8] += 2.f * E * dy * dz - (wy * dz + wz * dy) * j.inv5;
-                g[9] += E * dz * dz - wz * dz * j.inv5;
+            const f2x X = f2_bcast(s.cx[k]), Y = f2_bcast(s.cy[k]), Z = f2_bcast(s.cz[k]), M = f2_bcast(s.cm[k]);
+            const f2x qxx = f2_bcast(s.qxx[k]), qxy = f2_bcast(s.qxy[k]), qxz = f2_bcast(s.qxz[k]);
+            const f2x qyy = f2_bcast(s.qyy[k]), qyz = f2_bcast(s.qyz[k]), qzz = f2_bcast(s.qzz[k]);
+            f2x G[NADJ];
+#pragma unroll
+            for (int f = 0; f < NADJ; ++f) G[f] = f2_bcast(0.f);
+#pragma unroll 2
+            for (int i = 0; i < npe; i += 2) {
+                const f2x wx = ld2(s.iwx, i), wy = ld2(s.iwy, i), wz = ld2(s.iwz, i);
+                const f2x dx = f2_sub(X, ld2(s.ix, i)), dy = f2_sub(Y, ld2(s.iy, i)), dz = f2_sub(Z, ld2(s.iz, i));
+                const f2x inv = inv_r2<EPS0>(f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2))));
+                const CellJ2 j = cell_j2(dx, dy, dz, inv, M, qxx, qxy, qxz, qyy, qyz, qzz, wx, wy, wz);
+                G[0] = f2_fma(j.u, j.inv3, G[0]);
+                G[1] = f2_add(G[1], j.gdx);
+                G[2] = f2_add(G[2], j.gdy);
+                G[3] = f2_add(G[3], j.gdz);
+                // dQ: with E = 5/2 u / r^7 = D / 2 and p = -w / r^5,
+                //   dQ_kk += d_k (E d_k + p_k),  dQ_kl += d_l (D d_k + p_k) + p_l d_k  (k < l).
+                const f2x E = f2_mul(C05, j.D);
+                const f2x px = f2_mul(wx, j.n5), py = f2_mul(wy, j.n5), pz = f2_mul(wz, j.n5);
+                const f2x Dx = f2_fma(j.D, dx, px), Dy = f2_fma(j.D, dy, py);
+                G[4] = f2_fma(f2_fma(E, dx, px), dx, G[4]);
+                G[5] = f2_fma(Dx, dy, f2_fma(py, dx, G[5]));
+                G[6] = f2_fma(Dx, dz, f2_fma(pz, dx, G[6]));
+                G[7] = f2_fma(f2_fma(E, dy, py), dy, G[7]);
+                G[8] = f2_fma(Dy, dz, f2_fma(pz, dy, G[8]));
+                G[9] = f2_fma(f2_fma(E, dz, pz), dz, G[9]);
             }
             const uint32_t nd = s.clist[c0 + k];
 #pragma unroll
-            for (int f = 0; f < NADJ; ++f)
-                if (g[f] != 0.f) atomicAdd(a.nadj + f * T + nd, static_cast<double>(g[f]));
+            for (int f = 0; f < NADJ; ++f) {
+                const float g = f2_sum(G[f]);
+                if (g != 0.f) atomicAdd(a.nadj + f * T + nd, static_cast<double>(g));
+            }
         }
         __syncwarp();
     }
@@ -189,57 +248,83 @@ __device__ void vjp_flush(const VjpArgs& a, VjpSmem& s, int lane, int np, uint32
     const int total = range_prefix(s, nr, lane);
     for (int b0 = 0; b0 < total; b0 += VBCH) {
         const int bc = min(VBCH, total - b0);
+        for (int i = lane; i < np; i += 32) s.kself[i] = -2;
+        __syncwarp();
         for (int k = lane; k < bc; k += 32) {
             const uint32_t j = range_body(s, nr, b0 + k);
             const float4 h = a.hm[j], l = a.lo[j];
-            s.bx[k] = (h.x - ox) + l.x;
-            s.by[k] = (h.y - oy) + l.y;
-            s.bz[k] = (h.z - oz) + l.z;
+            const float X = (h.x - ox) + l.x, Y = (h.y - oy) + l.y, Z = (h.z - oz) + l.z;
+            s.bx[k] = X; s.by[k] = Y; s.bz[k] = Z;
             s.bm[k] = h.w;
             s.bj[k] = j;
+            if (j - plo < static_cast<uint32_t>(np)) s.kself[j - plo] = k;
+            if (k == bc - 1 && (bc & 1)) {
+                s.bx[bc] = X; s.by[bc] = Y; s.bz[bc] = Z;
+                s.bm[bc] = 0.f;
+                s.bj[bc] = 0xffffffffu;
+            }
         }
         __syncwarp();
-#pragma unroll
-        for (int u = 0; u < VIPT; ++u) {
-            const int i = lane + 32 * u;
-            if (i >= np) continue;
-            const uint32_t me = plo + i;
-            const float xi = s.ix[i], yi = s.iy[i], zi = s.iz[i], wx = s.iwx[i], wy = s.iwy[i], wz = s.iwz[i];
-            float ax = 0.f, ay = 0.f, az = 0.f;
-            for (int k = 0; k < bc; ++k) {
-                const float dx = s.bx[k] - xi, dy = s.by[k] - yi, dz = s.bz[k] - zi;
-                const float inv = inv_r<EPS0>(dx * dx + dy * dy + dz * dz + e2);
-                const float inv2 = inv * inv, inv3 = inv * inv2, inv5 = inv3 * inv2;
-                const float m = s.bj[k] == me ? 0.f : s.bm[k];
-                const float uw = wx * dx + wy * dy + wz * dz;
-                const float t = 3.f * uw * inv5;
-                ax += m * (wx * inv3 - t * dx);
-                ay += m * (wy * inv3 - t * dy);
-                az += m * (wz * inv3 - t * dz);
+        // i side: lanes over i-bodies, bodies two at a time (every P-th pair per partition). Per pair
+        //   gd = m_j (w_i / r^3 - 3 u d / r^5)  is summed as  w_i sum m_j / r^3 + sum (-3 m_j u / r^5) d.
+        for (int u = 0; u < nuP; ++u) {
+            const int i = lp + Lw * u;
+            const f2x xi = f2_bcast(s.ix[i]), yi = f2_bcast(s.iy[i]), zi = f2_bcast(s.iz[i]);
+            const f2x wx = f2_bcast(s.iwx[i]), wy = f2_bcast(s.iwy[i]), wz = f2_bcast(s.iwz[i]);
+            const int ks = i < np ? s.kself[i] : -2;
+            f2x ax = f2_bcast(0.f), ay = ax, az = ax, s3 = ax;
+#pragma unroll 2
+            for (int k = 2 * part; k < bc; k += 2 * P) {
+                f2x m = ld2(s.bm, k);
+                if (static_cast<unsigned>(ks - k) <= 1u) m = f2_mul(m, ks == k ? f2_pack(0.f, 1.f) : f2_pack(1.f, 0.f));
+                const f2x dx = f2_sub(ld2(s.bx, k), xi), dy = f2_sub(ld2(s.by, k), yi), dz = f2_sub(ld2(s.bz, k), zi);
+                const f2x inv = inv_r2<EPS0>(f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2))));
+                const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv, inv2), inv5 = f2_mul(inv3, inv2);
+                const f2x uw = f2_fma(wx, dx, f2_fma(wy, dy, f2_mul(wz, dz)));
+                const f2x t = f2_mul(f2_mul(CN3, f2_mul(m, uw)), inv5);
+                s3 = f2_fma(m, inv3, s3);
+                ax = f2_fma(t, dx, ax);
+                ay = f2_fma(t, dy, ay);
+                az = f2_fma(t, dz, az);
             }
-            kahan3(s, u, lane, ax, ay, az);
+            const float S = part_sum(f2_sum(s3), P);
+            const float sx = part_sum(f2_sum(ax), P), sy = part_sum(f2_sum(ay), P), sz = part_sum(f2_sum(az), P);
+            if (part == 0 && i < np) {
+                const float wxs = s.iwx[i], wys = s.iwy[i], wzs = s.iwz[i];
+                kahan3(s, i, fmaf(wxs, S, sx), fmaf(wys, S, sy), fmaf(wzs, S, sz));
+            }
         }
+        // Entry side: lanes over bodies, the group's i-bodies two at a time. Per pair
+        //   dx_j += m_j (w_i / r^3 - 3 u d / r^5),  dm_j += u / r^3  (m_j applied after the sum).
         for (int k = lane; k < bc; k += 32) {
             const uint32_t j = s.bj[k];
-            const float X = s.bx[k], Y = s.by[k], Z = s.bz[k], m = s.bm[k];
-            float gx = 0.f, gy = 0.f, gz = 0.f, gm = 0.f;
-            for (int i = 0; i < np; ++i) {
-                if (plo + i == j) continue;
-                const float wx = s.iwx[i], wy = s.iwy[i], wz = s.iwz[i];
-                const float dx = X - s.ix[i], dy = Y - s.iy[i], dz = Z - s.iz[i];
-                const float inv = inv_r<EPS0>(dx * dx + dy * dy + dz * dz + e2);
-                const float inv2 = inv * inv, inv3 = inv * inv2, inv5 = inv3 * inv2;
-                const float uw = wx * dx + wy * dy + wz * dz;
-                const float t = 3.f * uw * inv5;
-                gx += m * (wx * inv3 - t * dx);
-                gy += m * (wy * inv3 - t * dy);
-                gz += m * (wz * inv3 - t * dz);
-                gm += uw * inv3;
+            const int js = j - plo < static_cast<uint32_t>(np) ? static_cast<int>(j - plo) : -2;
+            const f2x X = f2_bcast(s.bx[k]), Y = f2_bcast(s.by[k]), Z = f2_bcast(s.bz[k]);
+            f2x GX = f2_bcast(0.f), GY = GX, GZ = GX, GM = GX;
+#pragma unroll 2
+            for (int i = 0; i < npe; i += 2) {
+                f2x wx = ld2(s.iwx, i), wy = ld2(s.iwy, i), wz = ld2(s.iwz, i);
+                if (static_cast<unsigned>(js - i) <= 1u) {
+                    const f2x msk = js == i ? f2_pack(0.f, 1.f) : f2_pack(1.f, 0.f);
+                    wx = f2_mul(wx, msk);
+                    wy = f2_mul(wy, msk);
+                    wz = f2_mul(wz, msk);
+                }
+                const f2x dx = f2_sub(X, ld2(s.ix, i)), dy = f2_sub(Y, ld2(s.iy, i)), dz = f2_sub(Z, ld2(s.iz, i));
+                const f2x inv = inv_r2<EPS0>(f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2))));
+                const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv, inv2), inv5 = f2_mul(inv3, inv2);
+                const f2x uw = f2_fma(wx, dx, f2_fma(wy, dy, f2_mul(wz, dz)));
+                const f2x t = f2_mul(f2_mul(CN3, uw), inv5);
+                GX = f2_fma(wx, inv3, f2_fma(t, dx, GX));
+                GY = f2_fma(wy, inv3, f2_fma(t, dy, GY));
+                GZ = f2_fma(wz, inv3, f2_fma(t, dz, GZ));
+                GM = f2_fma(uw, inv3, GM);
             }
-            atomicAdd(a.gx + j, static_cast<double>(gx));
-            atomicAdd(a.gy + j, static_cast<double>(gy));
-            atomicAdd(a.gz + j, static_cast<double>(gz));
-            atomicAdd(a.gm + j, static_cast<double>(gm));
+            const float m = s.bm[k];
+            atomicAdd(a.gx + j, static_cast<double>(m * f2_sum(GX)));
+            atomicAdd(a.gy + j, static_cast<double>(m * f2_sum(GY)));
+            atomicAdd(a.gz + j, static_cast<double>(m * f2_sum(GZ)));
+            atomicAdd(a.gm + j, static_cast<double>(f2_sum(GM)));
         }
         __syncwarp();
     }
@@ -263,12 +348,21 @@ __global__ void __launch_bounds__(VWBS) k_walk_vjp(VjpArgs a) {
             const int np = static_cast<int>(min(static_cast<uint32_t>(VPASS), gr.y - plo));
             for (int i = lane; i < np; i += 32) {
                 const float4 h = a.hm[plo + i], l = a.lo[plo + i], w = a.w[plo + i];
-                s.ix[i] = (h.x - bc.x) + l.x;
-                s.iy[i] = (h.y - bc.y) + l.y;
-                s.iz[i] = (h.z - bc.z) + l.z;
+                const float x = (h.x - bc.x) + l.x, y = (h.y - bc.y) + l.y, z = (h.z - bc.z) + l.z;
+                s.ix[i] = x;
+                s.iy[i] = y;
+                s.iz[i] = z;
                 s.iwx[i] = w.x;
                 s.iwy[i] = w.y;
                 s.iwz[i] = w.z;
+                if (i == np - 1 && (np & 1)) {  // zero-weight pad for the pairwise entry-side loops
+                    s.ix[np] = x;
+                    s.iy[np] = y;
+                    s.iz[np] = z;
+                    s.iwx[np] = 0.f;
+                    s.iwy[np] = 0.f;
+                    s.iwz[np] = 0.f;
+                }
             }
 #pragma unroll
             for (int u = 0; u < VIPT; ++u)
