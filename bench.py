@@ -551,8 +551,8 @@ def run_gb300(args, w, world, rank, local, dist):
     traffic = read_profile_traffic(args.workload)
 
     # End to end through the public API with host buffers: upload from page-locked memory, one
-    # step, download of the state, each step.
-    pin = PinnedBodies(n)
+    # step, download of the state into page-locked memory, each step.
+    pin, pin_out = PinnedBodies(n), PinnedBodies(n)
     hb = pin.bodies
     for f in ("x", "y", "z", "vx", "vy", "vz", "m", "id"):
         getattr(hb, f)[:] = getattr(b, f)
@@ -565,9 +565,10 @@ def run_gb300(args, w, world, rank, local, dist):
         be.upload(hb)
         be.compute_forces(p, False)
         step()
-        be.download()
+        be.download(pin_out.bodies)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     pin.free()
+    pin_out.free()
     e2e_ms = reduce_max(dist, e2e_ms)
 
     # CPU baseline (rank 0, N=1): the reference CPU algorithm on this host's cores, bounded sample.

@@ -357,8 +357,20 @@ class CudaBackend:
         _check(self._lib.lg_size(self._h, C.byref(n)))
         return int(n.value)
 
-    def download(self) -> Bodies:
-        out = Bodies.empty(self.size())
+    def download(self, out: Bodies | None = None) -> Bodies:
+        """The resident bodies in the backend's current order (src/backend.hpp:96). With ``out``
+        (for instance PinnedBodies(n).bodies) the arrays are written in place: each must be a
+        contiguous float32 (id: uint32) array of exactly size() elements."""
+        n = self.size()
+        if out is None:
+            out = Bodies.empty(n)
+        else:
+            for f in ("x", "y", "z", "vx", "vy", "vz", "m", "id"):
+                a = getattr(out, f)
+                want = np.uint32 if f == "id" else np.float32
+                if a.dtype != want or a.shape != (n,) or not a.flags.c_contiguous or not a.flags.writeable:
+                    raise ValueError(f"download: out.{f} must be a writable contiguous {np.dtype(want).name} "
+                                     f"array of {n} elements")
         _check(self._lib.lg_download(self._h, _fp(out.x), _fp(out.y), _fp(out.z), _fp(out.vx), _fp(out.vy),
                                      _fp(out.vz), _fp(out.m), _up(out.id)))
         return out

@@ -166,72 +166,98 @@ __device__ __forceinline__ int digit_at(const uint64_t* k0, const uint64_t* k1, 
 
 // ---- frame and keys --------------------------------------------------------------------------
 // frame: [0..2] origin, [3] side, [4] scale 2^21/side.
-__global__ void k_frame(const BodyArrays b, int n, double* partial, unsigned* ticket, double* frame) {
-    __shared__ double sh[6][BS / 32];
-    __shared__ bool last;
-    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) {
-        double p[3] = {b.x[i], b.y[i], b.z[i]};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            v[c] = fmin(v[c], p[c]);
-            v[3 + c] = fmax(v[3 + c], p[c]);
-        }
-    }
+// Bounding-box minima and maxima on the integer pipes: a double's bits mapped to a signed 64-bit
+// integer that orders as the values do (-0 below +0), NaN mapped to +inf for minima and to -inf
+// for maxima, so that it is ignored as fmin and fmax ignore it. FP64 issue is scarce on this part.
+__device__ __forceinline__ long long ord_bits(long long b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+__device__ __forceinline__ long long ord_lo(double d) {
+    const long long b = __double_as_longlong(d);
+    return nan_bits(b) ? 0x7ff0000000000000LL : ord_bits(b);
+}
+__device__ __forceinline__ long long ord_hi(double d) {
+    const long long b = __double_as_longlong(d);
+    return nan_bits(b) ? ord_bits(static_cast<long long>(0xfff0000000000000ULL)) : ord_bits(b);
+}
+__device__ __forceinline__ double ord_value(long long k) { return __longlong_as_double(ord_bits(k)); }
+
+// v[0..2] minima, v[3..5] maxima (ordered integers) of the block's bodies, reduced over the block
+// into sh (lane 0 of each warp) and returned by thread 0 in v.
+__device__ __forceinline__ void box_block_reduce(long long (&v)[6], long long (*sh)[BS / 32]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
         for (int o = 16; o > 0; o >>= 1) {
-            double t = __shfl_down_sync(0xffffffffu, v[c], o);
-            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
+            const long long t = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? min(v[c], t) : max(v[c], t);
         }
         if (lane == 0) sh[c][w] = v[c];
     }
     __syncthreads();
-    if (threadIdx.x < 6) {
-        const int c = threadIdx.x;
-        double r = sh[c][0];
-        for (int u = 1; u < BS / 32; ++u) r = c < 3 ? fmin(r, sh[c][u]) : fmax(r, sh[c][u]);
-        partial[blockIdx.x * 6 + c] = r;
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 6; ++c) {
+            long long r = sh[c][0];
+            for (int u = 1; u < BS / 32; ++u) r = c < 3 ? min(r, sh[c][u]) : max(r, sh[c][u]);
+            v[c] = r;
+        }
+}
+
+__device__ __forceinline__ void box_init(long long (&v)[6]) {
+    for (int c = 0; c < 3; ++c) {
+        v[c] = ord_bits(0x7ff0000000000000LL);                                   // +inf
+        v[3 + c] = ord_bits(static_cast<long long>(0xfff0000000000000ULL));      // -inf
     }
-    __syncthreads();
+}
+
+__device__ __forceinline__ void box_add(long long (&v)[6], double x, double y, double z) {
+    v[0] = min(v[0], ord_lo(x));
+    v[1] = min(v[1], ord_lo(y));
+    v[2] = min(v[2], ord_lo(z));
+    v[3] = max(v[3], ord_hi(x));
+    v[4] = max(v[4], ord_hi(y));
+    v[5] = max(v[5], ord_hi(z));
+}
+
+// src/cpu_backend.cpp:404-406: origin = the minima; side = max extent, widened by 1e-6; 1 if all
+// coincide; scale = 2^21 / side.
+__device__ __forceinline__ void write_frame(const long long (&v)[6], double* f) {
+    double r[6];
+    for (int c = 0; c < 6; ++c) r[c] = ord_value(v[c]);
+    double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
+    side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
+    f[0] = r[0];
+    f[1] = r[1];
+    f[2] = r[2];
+    f[3] = side;
+    f[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
+}
+
+__global__ void k_frame(const BodyArrays b, int n, long long* partial, unsigned* ticket, double* frame) {
+    __shared__ long long sh[6][BS / 32];
+    __shared__ bool last;
+    long long v[6];
+    box_init(v);
+    for (int i = blockIdx.x * BS + threadIdx.x; i < n; i += gridDim.x * BS) box_add(v, b.x[i], b.y[i], b.z[i]);
+    box_block_reduce(v, sh);
     if (threadIdx.x == 0) {
+        for (int c = 0; c < 6; ++c) partial[blockIdx.x * 6 + c] = v[c];
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double r[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    box_init(v);
     for (int blk = threadIdx.x; blk < static_cast<int>(gridDim.x); blk += BS)
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            const double t = __ldcg(&partial[blk * 6 + c]);
-            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
-        }
-#pragma unroll
-    for (int c = 0; c < 6; ++c)
-        for (int o = 16; o > 0; o >>= 1) {
-            const double t = __shfl_down_sync(0xffffffffu, r[c], o);
-            r[c] = c < 3 ? fmin(r[c], t) : fmax(r[c], t);
+            const long long t = __ldcg(&partial[blk * 6 + c]);
+            v[c] = c < 3 ? min(v[c], t) : max(v[c], t);
         }
     __syncthreads();
-    if (lane == 0)
-        for (int c = 0; c < 6; ++c) sh[c][w] = r[c];
-    __syncthreads();
+    box_block_reduce(v, sh);
     if (threadIdx.x == 0) {
-        for (int c = 0; c < 6; ++c) {
-            r[c] = sh[c][0];
-            for (int u = 1; u < BS / 32; ++u) r[c] = c < 3 ? fmin(r[c], sh[c][u]) : fmax(r[c], sh[c][u]);
-        }
-        // src/cpu_backend.cpp:404-406: side = max extent, widened by 1e-6; 1 if all coincide.
-        double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
-        side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
-        frame[0] = r[0];
-        frame[1] = r[1];
-        frame[2] = r[2];
-        frame[3] = side;
-        frame[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
+        write_frame(v, frame);
         *ticket = 0;
     }
 }
@@ -247,42 +273,13 @@ __global__ void k_keys(const uint32_t* __restrict__ sys, const BodyArrays b, int
 
 // Forest: one block per system computes its key frame over its body range [off[s], off[s + 1]).
 __global__ void k_frame_sys(const BodyArrays b, const uint32_t* __restrict__ off, double* frame) {
-    __shared__ double sh[6][BS / 32];
+    __shared__ long long sh[6][BS / 32];
     const uint32_t lo = off[blockIdx.x], hi = off[blockIdx.x + 1];
-    double v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    for (uint32_t i = lo + threadIdx.x; i < hi; i += BS) {
-        const double p[3] = {b.x[i], b.y[i], b.z[i]};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            v[c] = fmin(v[c], p[c]);
-            v[3 + c] = fmax(v[3 + c], p[c]);
-        }
-    }
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        for (int o = 16; o > 0; o >>= 1) {
-            const double t = __shfl_down_sync(0xffffffffu, v[c], o);
-            v[c] = c < 3 ? fmin(v[c], t) : fmax(v[c], t);
-        }
-        if (lane == 0) sh[c][w] = v[c];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double r[6];
-        for (int c = 0; c < 6; ++c) {
-            r[c] = sh[c][0];
-            for (int u = 1; u < BS / 32; ++u) r[c] = c < 3 ? fmin(r[c], sh[c][u]) : fmax(r[c], sh[c][u]);
-        }
-        double side = fmax(fmax(__dsub_rn(r[3], r[0]), __dsub_rn(r[4], r[1])), __dsub_rn(r[5], r[2]));
-        side = side > 0 ? __dmul_rn(side, 1 + 1e-6) : 1.0;
-        double* f = frame + 5 * blockIdx.x;
-        f[0] = r[0];
-        f[1] = r[1];
-        f[2] = r[2];
-        f[3] = side;
-        f[4] = __ddiv_rn(static_cast<double>(1u << MAX_LEVEL), side);
-    }
+    long long v[6];
+    box_init(v);
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += BS) box_add(v, b.x[i], b.y[i], b.z[i]);
+    box_block_reduce(v, sh);
+    if (threadIdx.x == 0) write_frame(v, frame + 5 * blockIdx.x);
 }
 
 // keys[i] = (system of body vals[i]): the second key of the forest's (system, Morton) sort.
@@ -1328,7 +1325,7 @@ void tree_sort(Engine& e) {
     } else {
         const int fb = std::min(2 * e.sms, grid_for(n, BS));
         e.diag_partial.reserve(static_cast<size_t>(fb) * 12 * 8);
-        k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<double>(), e.ticket(), t.frame.as<double>());
+        k_frame<<<fb, BS, 0, s>>>(e.bodies(e.cur), n, e.diag_partial.as<long long>(), e.ticket(), t.frame.as<double>());
     }
     LG_LAUNCHED();
     if (sys) t.mkeys.reserve(static_cast<size_t>(n) * 8 + 8);

@@ -181,3 +181,23 @@ def test_state_errors_and_empty_and_single(be):
     bad.nodes["child_count"] = 2
     with pytest.raises(ValueError):
         be.compute_forces_with(params(0, 0.01), False, remote=[bad])
+
+
+def test_download_into_page_locked_bodies(be):
+    b = S.plummer(3000, 21, cut=20)
+    be.upload(b)
+    be.compute_forces(params(1, 0.01), False)
+    be.kick(1e-3)
+    be.drift(1e-3)
+    want = be.download()
+    pin = L.backend.PinnedBodies(len(b))
+    try:
+        got = be.download(pin.bodies)
+        assert got is pin.bodies
+        for f in ("x", "y", "z", "vx", "vy", "vz", "m", "id"):
+            assert np.array_equal(getattr(got, f), getattr(want, f)), f
+        short = L.Bodies.empty(len(b) - 1)
+        with pytest.raises(ValueError):
+            be.download(short)
+    finally:
+        pin.free()
