@@ -112,7 +112,9 @@ __device__ __forceinline__ f2x pair_rsqrt(f2x r2) {
 }
 
 // Quadrupole cell terms: d points from the body to the cell,
-// a = G [M d/r^3 - Q d/r^5 + 5/2 (dQd) d/r^7], phi = -G [M/r + 1/2 dQd/r^5]. cc is even.
+// a = G [M d/r^3 - Q d/r^5 + 5/2 (dQd) d/r^7], phi = -G [M/r + 1/2 dQd/r^5]. cc is even. The
+// chunk holds -Q (negated when converted), which spares one negation per pair; sign changes are
+// exact, so the sums are those of the plain form bit for bit.
 template <int IPT, bool POT, bool EPS0>
 __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int k0, int kstep, int lane, const float (&xi)[IPT_MAX],
                                            const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
@@ -124,8 +126,7 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int k0, int kste
         ZI[u] = f2_bcast(zi[u]);
         ax[u] = ay[u] = az[u] = ap[u] = 0ull;
     }
-    const f2x E2 = f2_bcast(e2), C25 = f2_bcast(2.5f), NEG1 = f2_bcast(-1.f), C05 = f2_bcast(0.5f);
-    // Few i-bodies per lane leave little independent work per entry: unroll over entries then.
+    const f2x E2 = f2_bcast(e2), CN25 = f2_bcast(-2.5f), CN05 = f2_bcast(-0.5f);
 #pragma unroll CUNROLL
     for (int k = k0; k < cc; k += kstep) {
         const f2x X = ld2(s.cx + k), Y = ld2(s.cy + k), Z = ld2(s.cz + k), M = ld2(s.cm + k);
@@ -140,14 +141,13 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int k0, int kste
             const f2x qx = f2_fma(QXX, dx, f2_fma(QXY, dy, f2_mul(QXZ, dz)));
             const f2x qy = f2_fma(QXY, dx, f2_fma(QYY, dy, f2_mul(QYZ, dz)));
             const f2x qz = f2_fma(QXZ, dx, f2_fma(QYZ, dy, f2_mul(QZZ, dz)));
-            const f2x dqd = f2_fma(dx, qx, f2_fma(dy, qy, f2_mul(dz, qz)));
-            const f2x t5 = f2_mul(dqd, inv5);
-            const f2x f = f2_fma(M, inv3, f2_mul(f2_mul(C25, t5), inv2));
-            const f2x n5 = f2_mul(inv5, NEG1);
-            ax[u] = f2_fma(qx, n5, f2_fma(f, dx, ax[u]));
-            ay[u] = f2_fma(qy, n5, f2_fma(f, dy, ay[u]));
-            az[u] = f2_fma(qz, n5, f2_fma(f, dz, az[u]));
-            if (POT) ap[u] = f2_add(ap[u], f2_fma(M, inv, f2_mul(C05, t5)));
+            // qx, qy, qz = -(Q d); s5 = -(dQd) / r^5
+            const f2x s5 = f2_mul(f2_fma(dx, qx, f2_fma(dy, qy, f2_mul(dz, qz))), inv5);
+            const f2x f = f2_fma(M, inv3, f2_mul(f2_mul(CN25, s5), inv2));
+            ax[u] = f2_fma(qx, inv5, f2_fma(f, dx, ax[u]));
+            ay[u] = f2_fma(qy, inv5, f2_fma(f, dy, ay[u]));
+            az[u] = f2_fma(qz, inv5, f2_fma(f, dz, az[u]));
+            if (POT) ap[u] = f2_add(ap[u], f2_fma(M, inv, f2_mul(CN05, s5)));
         }
     }
 #pragma unroll
@@ -239,7 +239,8 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
                 s.cy[k] = (com.y - oy) + cl.y;
                 s.cz[k] = (com.z - oz) + cl.z;
                 s.cm[k] = com.w;
-                s.qxx[k] = q0.x; s.qxy[k] = q0.y; s.qxz[k] = q0.z; s.qyy[k] = q0.w; s.qyz[k] = q1.x; s.qzz[k] = q1.y;
+                s.qxx[k] = -q0.x; s.qxy[k] = -q0.y; s.qxz[k] = -q0.z; s.qyy[k] = -q0.w; s.qyz[k] = -q1.x;
+                s.qzz[k] = -q1.y;
             } else {
                 s.cx[k] = kFar; s.cy[k] = kFar; s.cz[k] = kFar; s.cm[k] = 0.f;
                 s.qxx[k] = s.qxy[k] = s.qxz[k] = s.qyy[k] = s.qyz[k] = s.qzz[k] = 0.f;
