@@ -543,7 +543,7 @@ def run_gb300(args, w, world, rank, local, dist):
     clocks = clk.summary()
 
     # Roofline of the dominant kernel (the walk): algorithmic flops / walk time.
-    # 20 flops per body-body pair, 65 per quadrupole cell term (per-unit counts in the design doc).
+    # 20 flops per body-body pair, 65 per quadrupole cell term (the GRAPE-style per-unit counts).
     if method == L.ForceMethod.tree:
         flops = [20.0 * a + 65.0 * c for a, c in zip(pairs, cells)]
     else:

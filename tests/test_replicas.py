@@ -1,5 +1,5 @@
-"""The multi-rank (replicas) path of bench.py on CPU: two gloo ranks on 127.0.0.1, as the driver's
-torchrun launch would start them. The single-system force path does not shard (replicas only):
+"""The multi-rank (replicas) path of bench.py on CPU: two gloo ranks on 127.0.0.1, as a
+`torch.distributed.run --nproc-per-node 2` launch starts them. The single-system force path does not shard (replicas only):
 every rank runs its own copy and rank 0 reports the slowest rank's time."""
 import json
 import os
