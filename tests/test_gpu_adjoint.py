@@ -101,10 +101,12 @@ def _by_id(be, cols):
     return out
 
 
-def test_tree_adjoint_theta0_equals_direct_adjoint(be):
-    """At theta = 0 every list is all bodies: the tree VJP is the pairwise VJP."""
+@pytest.mark.parametrize("eps", [0.03, 0.0])
+def test_tree_adjoint_theta0_equals_direct_adjoint(be, eps):
+    """At theta = 0 every list is all bodies: the tree VJP is the pairwise VJP (with eps = 0 both
+    take the unsoftened kernels, which drop the self pair by r = 0)."""
     b = S.plummer(600, 6, cut=10)
-    G, eps, dt, steps, every = 1.0, 0.03, 1e-3, 12, 4
+    G, dt, steps, every = 1.0, 1e-3, 12, 4
     rng = np.random.Generator(np.random.PCG64(6))
     xstar = b.pos64() + rng.normal(0, 1e-2, (len(b), 3))
     out = []
@@ -113,8 +115,10 @@ def test_tree_adjoint_theta0_equals_direct_adjoint(be):
         be.adjoint_forward(L.ForceParams(G=G, eps=eps, theta=0.0, method=method), dt, steps, every)
         out.append(be.adjoint_backward(xstar))
     (ld, gxd, gvd, gmd), (lt, gxt, gvt, gmt) = out
+    assert np.isfinite(gxt).all() and np.isfinite(gmt).all()
     assert abs(lt / ld - 1) <= 1e-6
-    assert _rel(gxt, gxd) <= 1e-5 and _rel(gvt, gvd) <= 1e-5 and _rel(gmt, gmd) <= 1e-5
+    tol = 1e-5 if eps > 0 else 1e-3  # unsoftened close pairs amplify FP32 rounding differences
+    assert _rel(gxt, gxd) <= tol and _rel(gvt, gvd) <= tol and _rel(gmt, gmd) <= tol
 
 
 def _engine_with_groups(mode):
