@@ -40,16 +40,29 @@ constexpr int WBS = 128;  // 4 warps per block
 constexpr int CUNROLL = LG_WALK_CUNROLL;
 constexpr int BUNROLL = LG_WALK_BUNROLL;
 constexpr int WARPS = WBS / 32;
-constexpr int CCH = 64;   // cells converted per chunk
-constexpr int BCH = 128;  // bodies converted per chunk
+#ifndef LG_WALK_CCH
+#define LG_WALK_CCH 160  // a whole flush of cells (CL_CAP) in one chunk
+#endif
+#ifndef LG_WALK_BCH
+#define LG_WALK_BCH 256
+#endif
+constexpr int CCH = LG_WALK_CCH;  // cells converted per chunk (a multiple of 8)
+constexpr int BCH = LG_WALK_BCH;  // bodies converted per chunk (a multiple of 8)
+static_assert(CCH % 8 == 0 && BCH % 8 == 0, "chunks hold whole pairs of every partition");
 constexpr int PASS = 128; // i-bodies per pass (4 per lane)
 
 constexpr int IPT_MAX = 4;
 
 // Per-warp shared memory. Chunks are struct-of-arrays so that entries k, k+1 load as one float2.
 struct __align__(16) WarpSmem {
-    float cx[CCH], cy[CCH], cz[CCH], cm[CCH], qxx[CCH], qxy[CCH], qxz[CCH], qyy[CCH], qyz[CCH], qzz[CCH];
-    float bx[BCH], by[BCH], bz[BCH], bm[BCH];
+    union {  // a flush converts its cells, then its bodies: the two chunks share the space
+        struct {
+            float cx[CCH], cy[CCH], cz[CCH], cm[CCH], qxx[CCH], qxy[CCH], qxz[CCH], qyy[CCH], qyz[CCH], qzz[CCH];
+        };
+        struct {
+            float bx[BCH], by[BCH], bz[BCH], bm[BCH];
+        };
+    };
     float ks[IPT_MAX][8][32];  // Kahan sums sx sy sz sp and compensations cx cy cz cp, per slot and lane
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];

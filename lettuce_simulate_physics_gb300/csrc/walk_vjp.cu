@@ -40,16 +40,30 @@ using namespace walk;
 
 constexpr int VWBS = 64;  // 2 warps per block
 constexpr int VWARPS = VWBS / 32;
-constexpr int VCCH = 64;
-constexpr int VBCH = 128;
+#ifndef LG_VJP_CCH
+#define LG_VJP_CCH 128
+#endif
+#ifndef LG_VJP_BCH
+#define LG_VJP_BCH 256
+#endif
+constexpr int VCCH = LG_VJP_CCH;  // cells per chunk (even)
+constexpr int VBCH = LG_VJP_BCH;  // bodies per chunk (even)
+static_assert(VCCH % 2 == 0 && VBCH % 2 == 0, "odd chunks are padded to whole pairs");
 constexpr int VPASS = 128;
 constexpr int VIPT = VPASS / 32;
 constexpr int NADJ = 10;  // per node: dM, dcom (3), dQ (xx, xy, xz, yy, yz, zz)
 
 struct __align__(16) VjpSmem {
-    float cx[VCCH], cy[VCCH], cz[VCCH], cm[VCCH], qxx[VCCH], qxy[VCCH], qxz[VCCH], qyy[VCCH], qyz[VCCH], qzz[VCCH];
-    float bx[VBCH], by[VBCH], bz[VBCH], bm[VBCH];
-    uint32_t bj[VBCH];
+    union {  // a flush converts its cells, then its bodies: the two chunks share the space
+        struct {
+            float cx[VCCH], cy[VCCH], cz[VCCH], cm[VCCH], qxx[VCCH], qxy[VCCH], qxz[VCCH], qyy[VCCH], qyz[VCCH],
+                qzz[VCCH];
+        };
+        struct {
+            float bx[VBCH], by[VBCH], bz[VBCH], bm[VBCH];
+            uint32_t bj[VBCH];
+        };
+    };
     float ix[VPASS], iy[VPASS], iz[VPASS], iwx[VPASS], iwy[VPASS], iwz[VPASS];
     int kself[VPASS];  // per i-body: its position in the current body chunk, or -2
     float ks[VIPT][6][32];  // i-side Kahan sums of gd (x, y, z) and compensations
