@@ -13,9 +13,11 @@
 //  - small N splits the j range over blockIdx.y (split-j); the slices' partials are summed in a
 //    fixed order by a second kernel, so results do not depend on scheduling.
 // Self interaction: with eps > 0 the self pair has d = 0 exactly (same relative coordinates), so
-// it adds nothing to a; its potential term m_i/eps is subtracted at the end. With eps == 0 the
-// r2 > 0 guard drops self and coincident pairs, as the reference does.
+// it adds nothing to a; for the potential it is excluded by index (its mass taken as zero in the
+// tiles that hold the block's own bodies). With eps == 0 the r2 > 0 guard drops self and
+// coincident pairs, as the reference does.
 #include <algorithm>
+#include <type_traits>
 #include <mutex>
 
 #include "engine.cuh"
@@ -57,7 +59,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
     const float4 oh = hm[base];
     const float4 ol = lo[base];
 
-    float xi[IPT], yi[IPT], zi[IPT], mself[IPT];
+    float xi[IPT], yi[IPT], zi[IPT];
     float sx[IPT], sy[IPT], sz[IPT], sp[IPT], cx[IPT], cy[IPT], cz[IPT], cp[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
@@ -66,7 +68,6 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
         xi[u] = (h.x - oh.x) + (l.x - ol.x);
         yi[u] = (h.y - oh.y) + (l.y - ol.y);
         zi[u] = (h.z - oh.z) + (l.z - ol.z);
-        mself[u] = h.w;
         sx[u] = sy[u] = sz[u] = sp[u] = 0.f;
         cx[u] = cy[u] = cz[u] = cp[u] = 0.f;
     }
@@ -139,30 +140,44 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
         const float* ry = sm.ry[buf];
         const float* rz = sm.rz[buf];
         const float* rm = sm.rm[buf];
+        // Pairs k, k + 1 of the tile. With the potential, the tiles that hold the block's own
+        // bodies take the self pair out by index (its mass half set to zero), as the reference's
+        // direct kernel does: no m/eps is added and subtracted, so phi keeps its low bits.
+        const int jt0 = j0 + t * TILE;
+        auto tile_pairs = [&](auto masked) {
+            constexpr bool MASK = decltype(masked)::value;
 #pragma unroll DUNROLL
-        for (int k = 0; k < cnt8; k += 2) {
-            const f2x X = *reinterpret_cast<const f2x*>(rx + k), Y = *reinterpret_cast<const f2x*>(ry + k);
-            const f2x Z = *reinterpret_cast<const f2x*>(rz + k), M = *reinterpret_cast<const f2x*>(rm + k);
+            for (int k = 0; k < cnt8; k += 2) {
+                const f2x X = *reinterpret_cast<const f2x*>(rx + k), Y = *reinterpret_cast<const f2x*>(ry + k);
+                const f2x Z = *reinterpret_cast<const f2x*>(rz + k), M = *reinterpret_cast<const f2x*>(rm + k);
 #pragma unroll
-            for (int u = 0; u < IPT; ++u) {
-                const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
-                const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
-                float r2a, r2b;
-                f2_unpack(r2, r2a, r2b);
-                float ia = rsqrt_mufu(r2a), ib = rsqrt_mufu(r2b);
-                if (EPS0) {
-                    ia = r2a > 0.f ? ia : 0.f;
-                    ib = r2b > 0.f ? ib : 0.f;
+                for (int u = 0; u < IPT; ++u) {
+                    f2x Mu = M;
+                    if (MASK) {
+                        const unsigned off = static_cast<unsigned>(base + u * DBS + tid - (jt0 + k));
+                        if (off <= 1u) Mu = f2_mul(M, off == 0 ? f2_pack(0.f, 1.f) : f2_pack(1.f, 0.f));
+                    }
+                    const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+                    const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+                    float r2a, r2b;
+                    f2_unpack(r2, r2a, r2b);
+                    float ia = rsqrt_mufu(r2a), ib = rsqrt_mufu(r2b);
+                    if (EPS0) {
+                        ia = r2a > 0.f ? ia : 0.f;
+                        ib = r2b > 0.f ? ib : 0.f;
+                    }
+                    const f2x inv = f2_pack(ia, ib);
+                    const f2x mi = f2_mul(Mu, inv);  // the self pair (d = 0) adds nothing to a
+                    const f2x f = f2_mul(mi, f2_mul(inv, inv));
+                    px[u] = f2_fma(f, dx, px[u]);
+                    py[u] = f2_fma(f, dy, py[u]);
+                    pz[u] = f2_fma(f, dz, pz[u]);
+                    if (POT) pp[u] = f2_add(pp[u], mi);
                 }
-                const f2x inv = f2_pack(ia, ib);
-                const f2x mi = f2_mul(M, inv);  // rounded: the self term cancels exactly
-                const f2x f = f2_mul(mi, f2_mul(inv, inv));
-                px[u] = f2_fma(f, dx, px[u]);
-                py[u] = f2_fma(f, dy, py[u]);
-                pz[u] = f2_fma(f, dz, pz[u]);
-                if (POT) pp[u] = f2_add(pp[u], mi);
             }
-        }
+        };
+        if (POT && jt0 < base + DBS * IPT && jt0 + cnt > base) tile_pairs(std::true_type{});
+        else tile_pairs(std::false_type{});
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             kahan_add(sx[u], cx[u], f2_sum(px[u]));
@@ -183,11 +198,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
     for (int u = 0; u < IPT; ++u) {
         const int i = base + u * DBS + tid;
         if (i >= n) continue;
-        float p = sp[u] - cp[u];
-        if (POT && !EPS0 && i >= j0 && i < j1) {
-            // The self pair's potential term, exactly as the loop formed it (r2 == e2).
-            p = __fsub_rn(p, __fmul_rn(mself[u], rsqrt_mufu(e2)));
-        }
+        const float p = sp[u] - cp[u];
         if (write_final) {
             out[i] = make_float4(G * (sx[u] - cx[u]), G * (sy[u] - cy[u]), G * (sz[u] - cz[u]), POT ? -G * p : 0.f);
             if (cost) cost[i] = static_cast<float>(n - 1);  // interactions: every other body

@@ -64,6 +64,7 @@ struct __align__(16) WarpSmem {
         };
     };
     float ks[IPT_MAX][8][32];  // Kahan sums sx sy sz sp and compensations cx cy cz cp, per slot and lane
+    int kself[PASS];           // with the potential: each i-body's position in the body chunk, or -2
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];
     uint32_t rpre[RL_CAP + 1];
@@ -168,10 +169,12 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cc, int k0, int kste
 }
 
 // Softened body terms a = G m d / r^3, phi = -G m / r. bc is even.
+// With the potential, the own body's pair is taken out by index (its mass half set to zero):
+// kself[u] is the chunk position of the lane's u-th i-body (-2: not in this chunk).
 template <int IPT, bool POT, bool EPS0>
 __device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int k0, int kstep, int lane,
                                             const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
-                                            const float (&zi)[IPT_MAX], float e2) {
+                                            const float (&zi)[IPT_MAX], const int (&kself)[IPT_MAX], float e2) {
     f2x XI[IPT], YI[IPT], ZI[IPT], ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
@@ -186,10 +189,15 @@ __device__ __forceinline__ void eval_bodies(WarpSmem& s, int bc, int k0, int kst
         const f2x X = ld2(s.bx + k), Y = ld2(s.by + k), Z = ld2(s.bz + k), M = ld2(s.bm + k);
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
+            f2x Mu = M;
+            if (POT) {
+                const unsigned off = static_cast<unsigned>(kself[u] - k);
+                if (off <= 1u) Mu = f2_mul(M, off == 0 ? f2_pack(0.f, 1.f) : f2_pack(1.f, 0.f));
+            }
             const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
             const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
             const f2x inv = pair_rsqrt<EPS0>(r2);
-            const f2x mi = f2_mul(M, inv);  // rounded: the self term cancels exactly
+            const f2x mi = f2_mul(Mu, inv);  // the self pair (d = 0) adds nothing to a
             const f2x f = f2_mul(mi, f2_mul(inv, inv));
             ax[u] = f2_fma(f, dx, ax[u]);
             ay[u] = f2_fma(f, dy, ay[u]);
@@ -216,12 +224,12 @@ __device__ __forceinline__ void eval_cells_n(int ipt, WarpSmem& s, int cc, int k
 template <bool POT, bool EPS0>
 __device__ __forceinline__ void eval_bodies_n(int ipt, WarpSmem& s, int bc, int k0, int kstep, int lane,
                                               const float (&xi)[IPT_MAX], const float (&yi)[IPT_MAX],
-                                              const float (&zi)[IPT_MAX], float e2) {
+                                              const float (&zi)[IPT_MAX], const int (&kself)[IPT_MAX], float e2) {
     switch (ipt) {
-        case 1: eval_bodies<1, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
-        case 2: eval_bodies<2, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
-        case 3: eval_bodies<3, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
-        default: eval_bodies<4, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 1: eval_bodies<1, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        case 2: eval_bodies<2, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        case 3: eval_bodies<3, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        default: eval_bodies<4, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
     }
 }
 
@@ -232,7 +240,8 @@ constexpr float kFar = 1e18f;
 template <bool POT, bool EPS0>
 __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, int ipt, int part, int P, int nc,
                                       int nr, float ox, float oy, float oz, const float (&xi)[IPT_MAX],
-                                      const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2) {
+                                      const float (&yi)[IPT_MAX], const float (&zi)[IPT_MAX], float e2, uint32_t plo,
+                                      int np) {
     const int pad = 2 * P - 1;  // chunks padded to whole pairs per partition
     for (int c0 = 0; c0 < nc; c0 += CCH) {
         const int cc = min(CCH, nc - c0);
@@ -265,12 +274,18 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
     }
     if (nr == 0) return;
     const int total = range_prefix(s, nr, lane);
+    const int Lw = 32 / P, lp = lane % Lw;
     for (int b0 = 0; b0 < total; b0 += BCH) {
         const int bc = min(BCH, total - b0);
         const int bc2 = (bc + pad) & ~pad;
+        if (POT) {
+            for (int i = lane; i < np; i += 32) s.kself[i] = -2;
+            __syncwarp();
+        }
         for (int k = lane; k < bc2; k += 32) {
             if (k < bc) {
                 const uint32_t j = range_body(s, nr, b0 + k);
+                if (POT && j - plo < static_cast<uint32_t>(np)) s.kself[j - plo] = k;
                 float4 h, l;
                 if (j & REMOTE) {
                     h = w.let.body[j & ~REMOTE];
@@ -288,7 +303,13 @@ __device__ __forceinline__ void flush(const WalkArgs& w, WarpSmem& s, int lane, 
             }
         }
         __syncwarp();
-        eval_bodies_n<POT, EPS0>(ipt, s, bc2, 2 * part, 2 * P, lane, xi, yi, zi, e2);
+        int kself[IPT_MAX];
+#pragma unroll
+        for (int u = 0; u < IPT_MAX; ++u) {
+            const int i = lp + Lw * u;
+            kself[u] = POT && i < np ? s.kself[i] : -2;
+        }
+        eval_bodies_n<POT, EPS0>(ipt, s, bc2, 2 * part, 2 * P, lane, xi, yi, zi, kself, e2);
         __syncwarp();
     }
 }
@@ -315,7 +336,7 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         }
     }
     const int Lw = 32 / P, part = lane / Lw, lp = lane % Lw;
-    float xi[IPT_MAX], yi[IPT_MAX], zi[IPT_MAX], mi[IPT_MAX];
+    float xi[IPT_MAX], yi[IPT_MAX], zi[IPT_MAX];
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
         const int k = min(lp + Lw * u, np - 1);
@@ -323,7 +344,6 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         xi[u] = (h.x - ox) + l.x;
         yi[u] = (h.y - oy) + l.y;
         zi[u] = (h.z - oz) + l.z;
-        mi[u] = h.w;
     }
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u)
@@ -333,16 +353,15 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
     const float e2 = w.e2_sys ? w.e2_sys[root] : w.e2;
     uint32_t list_len = 0, cells_len = 0;
     auto fl = [&](int nc, int nr) {
-        flush<POT, EPS0>(w, s, lane, ipt, part, P, nc, nr, ox, oy, oz, xi, yi, zi, e2);
+        flush<POT, EPS0>(w, s, lane, ipt, part, P, nc, nr, ox, oy, oz, xi, yi, zi, e2, plo, np);
     };
     if (w.local) traverse(w.tv, s, stack, lane, gr, bc, bh, root, w.err, list_len, cells_len, fl);
     for (int t = 0; t < w.let.ntrees; ++t)
         traverse_let(w.let, s, stack, lane, bc, bh, w.let.roots[t], w.err, list_len, cells_len, fl);
     // With the local tree the own body is in the list (its leaf is inside the group, so it is
-    // opened): it is not an interaction, and with eps > 0 its pair (d = 0) only adds m_i/eps to the
-    // potential, which is taken out. Remote trees never hold the target.
+    // opened): it is not an interaction, adds nothing to a (d = 0) and is excluded from the
+    // potential by index. Remote trees never hold the target.
     const uint32_t self = w.local ? 1u : 0u;
-    const float self_inv = (POT && !EPS0) ? rsqrt_mufu(e2) : 0.f;
 #pragma unroll
     for (int u = 0; u < IPT_MAX; ++u) {
         const float* ks = &s.ks[u][0][lane];
@@ -357,7 +376,6 @@ __device__ void walk_pass(const WalkArgs& w, WarpSmem& s, uint32_t* stack, int l
         const int k = lp + Lw * u;
         if (part != 0 || k >= np) continue;
         const uint32_t i = plo + k;
-        if (POT && !EPS0 && w.local) p = __fsub_rn(p, __fmul_rn(mi[u], self_inv));
         const float4 a = make_float4(w.G * fx, w.G * fy, w.G * fz, POT ? -w.G * p : 0.f);
         if (w.accumulate) {
             const float4 o = w.acc[i];
