@@ -213,3 +213,42 @@ def test_compute_forces_equals_build_and_empty_remote(engines, method):
     be.compute_forces_with(p, True, [])
     a1 = accel_by_id(be, len(b))
     assert np.array_equal(a0, a1) and be.diagnostics().pe == pe0
+
+
+@pytest.mark.parametrize("theta", [0.6, 0.4])
+def test_four_way_quadrant_split(theta):
+    """tests/test_cpu_let.cpp:101-174 (4-way split): four engines, one per quadrant of x-y; each
+    takes the LETs of the other three. Relative rms vs the FP64 direct sum <= 1.5e-3 (theta 0.6) or
+    4e-4 (theta 0.4); total potential energy within 2e-3."""
+    from lettuce_simulate_physics_gb300 import build as B
+    B.build()
+    all_b = zero_v(S.plummer(20000, 13, cut=20))
+    N = len(all_b)
+    ref = O.direct_fp64(all_b, 1.0, 0.01)
+    pe_ref = 0.5 * float((all_b.m.astype(np.float64) * ref[3]).sum())
+    part = (all_b.x >= 0).astype(int) + 2 * (all_b.y >= 0).astype(int)
+    p = params(1, theta=theta)
+    bes = [L.CudaBackend(0) for _ in range(4)]
+    try:
+        for q, be in enumerate(bes):
+            be.upload(all_b.subset(part == q))
+            be.build_tree(p)
+        boxes = [be.local_bounds() for be in bes]
+        a = np.zeros((4, N))
+        pe = 0.0
+        for i, be in enumerate(bes):
+            remote = [bes[j].export_let(boxes[i].lo, boxes[i].hi, p) for j in range(4) if j != i]
+            be.compute_forces_with(p, True, remote)
+            out = be.download()
+            a[:, out.id] = be.accel()
+            ok, c = be.body_costs()
+            assert ok and float(c.astype(np.float64).sum()) == float(be.times().interactions)
+            pe += be.diagnostics().pe
+        e = rel_rms(a[:3], ref[:3])
+        print(f"4-way theta {theta}: rel rms {e:.3g}, pe rel {abs(pe / pe_ref - 1):.3g}")
+        assert np.isfinite(a).all()
+        assert e <= (1.5e-3 if theta > 0.5 else 4e-4)
+        assert abs(pe / pe_ref - 1) <= 2e-3
+    finally:
+        for be in bes:
+            be.close()

@@ -45,3 +45,21 @@ def test_render_rejects_bad_views_and_sizes(be):
         be.render(16, 16, view="sideways")
     with pytest.raises(ValueError):
         be.render(0, 16)
+
+
+def test_non_finite_bodies_are_skipped(be):
+    """tests/test_render.cpp:83-105: non-finite bodies do not poison the frame."""
+    t = np.arange(200) * 0.3
+    pos = np.stack([np.cos(t), np.sin(t), np.zeros(200)], 1)
+    clean = L.Bodies.from_arrays(pos, np.zeros((200, 3)), np.ones(200))
+    be.upload(clean)
+    rgb0, ext0 = be.render(64, 64)
+    bad_pos = np.array([[np.nan, 0, 0], [0, np.inf, 0], [0, 0, 0]])
+    bad_vel = np.array([[0, 0, 0], [0, 0, 0], [np.nan, 0, 0]])
+    dirty = clean.append(L.Bodies.from_arrays(bad_pos, bad_vel, np.ones(3)))
+    be.upload(dirty)
+    rgb1, ext1 = be.render(64, 64)
+    assert abs(ext1 - ext0) <= 0.01
+    assert int((rgb1 > 40).sum()) > 50
+    _, ext_speed = be.render(64, 64, color="speed")
+    assert ext_speed > 0
