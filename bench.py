@@ -484,6 +484,39 @@ def run_reference(args, w, world, rank, dist):
     return 0
 
 
+# Algorithmic bytes per body of the tree step's memory-side phases (this engine's layout):
+#   sort:  bounding box (read FP64 x, y, z: 24), keys (read 24, write key 8 + index 4), histogram
+#          (read keys 8), eight onesweep passes (read and write key + index: 24 each), permute (read
+#          and write the body arrays, 81 B each way, plus the index 4);
+#   build: keys read once (8), positions and masses read once by the leaf moments (32), node
+#          records written once (about N/4 nodes x 96 B: range, geometry, moments).
+SORT_BYTES_PER_BODY = 24 + 36 + 8 + 8 * 24 + 2 * 81 + 4
+BUILD_BYTES_PER_BODY = 8 + 32 + 24
+
+
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth of the GB300s, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def phase_roofline(n, sort_ms, build_ms):
+    peak, src = hbm_peak()
+    out = {}
+    for name, per, t in (("sort", SORT_BYTES_PER_BODY, sort_ms), ("build", BUILD_BYTES_PER_BODY, build_ms)):
+        gbs = n * per / (t * 1e-3) / 1e9 if t > 0 else None
+        out[name] = {"bound": "hbm", "bytes_per_body": per, "achieved": round(gbs, 1) if gbs else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4) if gbs else None,
+                     "peak_source": src}
+    out["build"]["note"] = ("FP64-latency bound in practice: the moments upsweep (leaf moments and one "
+                            "launch per tree level) is about half of the phase")
+    out["sort"]["note"] = "eight dependent onesweep passes, each limited by its decoupled look-back"
+    return out
+
+
 def run_gb300(args, w, world, rank, local, dist):
     import lettuce_simulate_physics_gb300 as L
     from lettuce_simulate_physics_gb300 import build as B
@@ -606,6 +639,8 @@ def run_gb300(args, w, world, rank, local, dist):
             "interactions_per_step": int(statistics.fmean(inter)),
             "ginteractions_per_s": round(statistics.fmean(inter) / (statistics.fmean(force_ms) * 1e-3) / 1e9, 2),
             "force_error_vs_fp64": {"median": err_med, "p99": err_p99, "sample_bodies": 256},
+            "phase_roofline": phase_roofline(n, statistics.fmean(sort_ms), statistics.fmean(build_ms))
+            if method == L.ForceMethod.tree else None,
             "roofline": {"bound": "fp32", "kernel": "walk" if method == L.ForceMethod.tree else "direct",
                          "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
                          "frac": round(achieved / peak, 4) if peak else None, "traffic": traffic,
