@@ -36,11 +36,12 @@ def test_reduce_max_and_barrier_over_two_gloo_ranks(tmp_path):
         "world, rank, local, dist = bench.dist_setup()\n"
         "bench.barrier(dist)\n"
         "m = bench.reduce_max(dist, 10.0 + rank)\n"
-        "print('RANK', rank, world, m, flush=True)\n")
+        f"open(os.path.join({str(tmp_path)!r}, f'rank{{rank}}.txt'), 'w').write(f'{{rank}} {{world}} {{m}}')\n")
     r = torchrun([str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("RANK")]
-    assert sorted(lines) == ["RANK 0 2 11.0", "RANK 1 2 11.0"]
+    # One file per rank: the ranks' stdout streams interleave.
+    got = sorted((tmp_path / f"rank{k}.txt").read_text() for k in range(2))
+    assert got == ["0 2 11.0", "1 2 11.0"]
 
 
 def test_reference_arm_prints_one_line_from_rank_zero():
