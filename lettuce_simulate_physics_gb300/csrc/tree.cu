@@ -58,6 +58,10 @@ constexpr int SORT_BS = 256;
 constexpr int SORT_IPT = LG_SORT_IPT;  // keys per thread of a sort tile
 constexpr int SORT_TILE = SORT_BS * SORT_IPT;
 constexpr unsigned FLAG_AGG = 1u << 30, FLAG_INC = 2u << 30, VAL_MASK = (1u << 30) - 1;
+#ifndef LG_LB_BATCH
+#define LG_LB_BATCH 4
+#endif
+constexpr int LB_BATCH = LG_LB_BATCH;  // predecessors read per look-back round trip
 
 struct SortCtl {
     unsigned sel;
@@ -405,20 +409,32 @@ __global__ void __launch_bounds__(SORT_BS) k_sort_pass(uint64_t* __restrict__ kA
             lb[d] = FLAG_INC | tile_count;
         } else {
             lb[d] = FLAG_AGG | tile_count;
+            // Look back LB_BATCH predecessors per round trip: their flags are read together and
+            // taken in order (aggregates added until an inclusive prefix; an unpublished tile is
+            // waited for, keeping what was added before it).
             int j = static_cast<int>(tile) - 1;
             unsigned spins = 0;
             while (j >= 0) {
-                const unsigned sv = *reinterpret_cast<volatile const unsigned*>(&lookback[static_cast<size_t>(j) * RADIX + d]);
-                if (sv & FLAG_INC) {
-                    prefix += sv & VAL_MASK;
-                    break;
+                unsigned sv[LB_BATCH];
+#pragma unroll
+                for (int q = 0; q < LB_BATCH; ++q)
+                    sv[q] = j - q >= 0 ? *reinterpret_cast<volatile const unsigned*>(
+                                             &lookback[static_cast<size_t>(j - q) * RADIX + d])
+                                       : FLAG_INC;
+                int taken = 0;
+                bool inc = false;
+#pragma unroll
+                for (int q = 0; q < LB_BATCH; ++q) {
+                    if (inc || taken < q) break;
+                    if (sv[q] & (FLAG_INC | FLAG_AGG)) {
+                        prefix += sv[q] & VAL_MASK;
+                        inc = (sv[q] & FLAG_INC) != 0;
+                        ++taken;
+                    }
                 }
-                if (sv & FLAG_AGG) {
-                    prefix += sv & VAL_MASK;
-                    --j;
-                    continue;
-                }
-                if (++spins > kSpinCap) {
+                if (inc) break;
+                j -= taken;
+                if (taken == 0 && ++spins > kSpinCap) {
                     atomicOr(err, kErrWaitTimeout);
                     break;
                 }
@@ -559,11 +575,27 @@ __global__ void __launch_bounds__(SCAN_BS) k_scan(const uint32_t* __restrict__ i
             st[tile] = SFLAG_AGG | block_total;
             long long j = static_cast<long long>(tile) - 1;
             unsigned spins = 0;
-            while (j >= 0) {
-                const unsigned long long s = st[j];
-                if (s & SFLAG_INC) { prefix += s & SVAL; break; }
-                if (s & SFLAG_AGG) { prefix += s & SVAL; --j; continue; }
-                if (++spins > kSpinCap) { atomicOr(err, kErrWaitTimeout); break; }
+            while (j >= 0) {  // LB_BATCH predecessors per round trip, taken in order (as in the sort)
+                unsigned long long sv[LB_BATCH];
+#pragma unroll
+                for (int q = 0; q < LB_BATCH; ++q) {
+                    const unsigned long long v = j - q >= 0 ? st[j - q] : 0ull;
+                    sv[q] = j - q >= 0 ? v : static_cast<unsigned long long>(SFLAG_INC);
+                }
+                int taken = 0;
+                bool inc = false;
+#pragma unroll
+                for (int q = 0; q < LB_BATCH; ++q) {
+                    if (inc || taken < q) break;
+                    if (sv[q] & (SFLAG_INC | SFLAG_AGG)) {
+                        prefix += sv[q] & SVAL;
+                        inc = (sv[q] & SFLAG_INC) != 0;
+                        ++taken;
+                    }
+                }
+                if (inc) break;
+                j -= taken;
+                if (taken == 0 && ++spins > kSpinCap) { atomicOr(err, kErrWaitTimeout); break; }
             }
             st[tile] = SFLAG_INC | ((prefix + block_total) & SVAL);
         }
