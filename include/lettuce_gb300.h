@@ -230,6 +230,11 @@ lg_status lg_interaction_split(lg_engine* e, uint64_t* body_pairs, uint64_t* cel
  * with CUDA events on the engine's stream), in TFLOP/s: the roofline denominator of the force
  * kernels. */
 lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops);
+/* Self-test of failure detection (no reference counterpart): one block waits on an mbarrier no one
+ * arrives on and on a flag no one sets, `polls` polls each (1 .. 2^20), with the bounded-wait
+ * primitives the kernels use. Both waits give up; the call returns LG_ERR_RUNTIME with "device wait
+ * timed out" in lg_last_error(), the error word is cleared and the engine stays usable. */
+lg_status lg_probe_wait_timeout(lg_engine* e, unsigned polls);
 /* Page-locked host memory for transfers that overlap (cudaMallocHost / cudaFreeHost). */
 lg_status lg_host_alloc(size_t bytes, void** out);
 lg_status lg_host_free(void* p);

@@ -212,6 +212,7 @@ def _lib() -> C.CDLL:
         "lg_launch_count": (st, [vp, C.POINTER(C.c_uint64)]),
         "lg_interaction_split": (st, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "lg_probe_fp32_peak": (st, [vp, C.POINTER(C.c_double)]),
+        "lg_probe_wait_timeout": (st, [vp, C.c_uint]),
         "lg_host_alloc": (st, [C.c_size_t, C.POINTER(vp)]),
         "lg_adjoint_forward": (st, [vp, C.POINTER(_CForceParams), C.c_double, C.c_int, C.c_int]),
         "lg_adjoint_backward": (st, [vp, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d, _d]),
@@ -524,6 +525,12 @@ class CudaBackend:
         t = C.c_double()
         _check(self._lib.lg_probe_fp32_peak(self._h, C.byref(t)))
         return float(t.value)
+
+    def probe_wait_timeout(self, polls: int = 4096) -> None:
+        """Self-test of failure detection: device waits that are never satisfied give up after
+        `polls` polls and the call raises RuntimeError("... device wait timed out ..."); the engine
+        stays usable."""
+        _check(self._lib.lg_probe_wait_timeout(self._h, int(polls)))
 
     def adjoint_forward(self, p: ForceParams, dt: float, steps: int, checkpoint_every: int) -> None:
         """Runs `steps` KDK steps from the resident state, keeping adjoint checkpoints."""

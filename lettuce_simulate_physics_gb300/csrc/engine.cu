@@ -853,6 +853,21 @@ lg_status lg_probe_fp32_peak(lg_engine* e, double* tflops) {
     });
 }
 
+lg_status lg_probe_wait_timeout(lg_engine* e, unsigned polls) {
+    return guard([&] {
+        Engine& E = eng(e);
+        if (polls < 1 || polls > (1u << 20)) lg::fail(lg::kArg, "probe_wait_timeout: polls must be in [1, 2^20]");
+        LG_CK(cudaSetDevice(E.dev));
+        // small[16..19] stays zero here: the flag no one sets.
+        LG_CK(cudaMemsetAsync(E.small.as<char>(), 0, 32, E.stream));
+        lg::probe_waits(E.stream, polls, E.small.as<unsigned>() + 4 + 0, E.err_word());
+        ++E.launches;
+        LG_CK(cudaMemcpyAsync(E.pinned_small, E.small.as<char>(), 4, cudaMemcpyDeviceToHost, E.stream));
+        LG_CK(cudaStreamSynchronize(E.stream));
+        E.check_device_errors("wait probe");
+    });
+}
+
 lg_status lg_adjoint_forward(lg_engine* e, const lg_force_params* p, double dt, int steps, int checkpoint_every) {
     return guard([&] {
         need(p, "params");

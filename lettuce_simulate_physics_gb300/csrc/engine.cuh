@@ -203,5 +203,6 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
 void render(Engine& e, const lg_render_options& o, unsigned char* rgb, double* extent_used);
 // integrate.cu
 double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink);
+void probe_waits(cudaStream_t s, unsigned polls, const unsigned* never_set, unsigned* err);
 
 }  // namespace lg

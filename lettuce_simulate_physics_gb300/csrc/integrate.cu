@@ -312,7 +312,31 @@ __global__ void k_ffma_probe(int iters, float seed, unsigned* sink) {
     if (s == 12345.678f) atomicAdd(sink, 1u);  // keeps the chains live
 }
 
+// Self-test of the bounded waits: an mbarrier no one arrives on and a flag no one sets, each
+// waited on with `polls` polls by the primitives the kernels use (mbar_wait_bounded as in the
+// direct kernels' TMA pipeline, a volatile flag poll as in the sort and scan look-backs). Both give
+// up, record kErrWaitTimeout in the error word and return; nothing is left in flight.
+__global__ void k_probe_waits(unsigned polls, const unsigned* never_set, unsigned* err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    if (!mbar_wait_bounded(&bar, 0, polls)) atomicOr(err, kErrWaitTimeout);
+    unsigned it = 0;
+    while (*reinterpret_cast<volatile const unsigned*>(never_set) == 0u && ++it < polls) {
+    }
+    if (it >= polls) atomicOr(err, kErrWaitTimeout);
+}
+
 }  // namespace
+
+void probe_waits(cudaStream_t s, unsigned polls, const unsigned* never_set, unsigned* err) {
+    k_probe_waits<<<1, 32, 0, s>>>(polls, never_set, err);
+    LG_LAUNCHED();
+}
 
 double probe_fp32_peak(cudaStream_t s, int sms, unsigned* sink) {
     const int blocks = sms * 8, threads = 256, iters = 1 << 14;

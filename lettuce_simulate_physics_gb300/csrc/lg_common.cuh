@@ -122,9 +122,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     return ok != 0;
 }
 
-// Bounded wait for the barrier phase `parity` to complete; false after kSpinCap polls.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-    for (unsigned it = 0; it < kSpinCap; ++it)
+// Bounded wait for the barrier phase `parity` to complete; false after `cap` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned cap = kSpinCap) {
+    for (unsigned it = 0; it < cap; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -201,3 +201,21 @@ def test_download_into_page_locked_bodies(be):
             be.download(short)
     finally:
         pin.free()
+
+
+def test_bounded_waits_report_timeout_and_engine_stays_usable(be):
+    """Failure detection without a GPU fault: waits that nothing satisfies (an mbarrier no one
+    arrives on, a flag no one sets) give up after their poll limit, the host reports "device wait
+    timed out", the error word is cleared and the next force call is unaffected."""
+    b = S.plummer(2000, 41)
+    p = params(1, 0.01)
+    be.upload(b)
+    be.compute_forces(p, True)
+    a0, pe0 = be.accel(), be.diagnostics().pe
+    with pytest.raises(RuntimeError, match="device wait timed out"):
+        be.probe_wait_timeout(2048)
+    be.upload(b)
+    be.compute_forces(p, True)
+    assert np.array_equal(be.accel(), a0) and be.diagnostics().pe == pe0
+    with pytest.raises(ValueError):
+        be.probe_wait_timeout(0)
