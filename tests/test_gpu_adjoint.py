@@ -122,16 +122,32 @@ def test_tree_adjoint_theta0_equals_direct_adjoint(be, eps):
 
 
 def _engine_with_groups(mode):
+    """mode: "reference" or "merged" walk groups, or "groupN": reference groups of up to N bodies
+    (N > 128 makes the walk and its VJP take several passes per group)."""
     import os
-    old = os.environ.get("LETTUCE_GB300_WALK_GROUPS")
-    os.environ["LETTUCE_GB300_WALK_GROUPS"] = mode
+    env = {"LETTUCE_GB300_WALK_GROUPS": "reference", "LETTUCE_CUDA_GROUP": None}
+    if mode.startswith("group"):
+        env["LETTUCE_CUDA_GROUP"] = mode[5:]
+    else:
+        env["LETTUCE_GB300_WALK_GROUPS"] = mode
+    old = {k: os.environ.get(k) for k in env}
     try:
+        for k, v in env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
         return L.CudaBackend(0)
     finally:
-        os.environ["LETTUCE_GB300_WALK_GROUPS"] = old if old is not None else "reference"
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
-@pytest.mark.parametrize("theta,groups", [(0.6, "reference"), (0.3, "reference"), (0.6, "merged")])
+@pytest.mark.parametrize("theta,groups", [(0.6, "reference"), (0.3, "reference"), (0.6, "merged"),
+                                          (0.6, "group256")])
 def test_tree_adjoint_vs_frozen_list_central_differences(be, theta, groups):
     be = _engine_with_groups(groups)
     b = S.plummer(3000, 4, cut=10)

@@ -348,3 +348,27 @@ def test_fp64_sidecar_restart_continues_bit_for_bit(be, tmp_path):
     for f in ("vx", "vy", "vz", "id"):
         assert np.array_equal(getattr(a, f), getattr(c, f)), f
     other.close()
+
+
+@pytest.mark.parametrize("group", ["512", "1024"])
+def test_groups_larger_than_one_pass(group):
+    """LETTUCE_CUDA_GROUP above 128: a walk group spans several passes of 128 i-bodies, each with
+    its own traversal of the group's list. Accuracy as the reference groups (relative rms vs the
+    FP64 direct sum <= 1e-3), costs sum to the interactions, larger groups open more cells."""
+    b = S.plummer(20000, 2, cut=20)
+    exact = O.direct_fp64(b, 1.0, 0.01)
+    ref_a = by_id(b.id, exact[:3])
+    big = with_env({"LETTUCE_CUDA_GROUP": group})
+    base = with_env({})
+    try:
+        assert big.name().endswith(f"group walk {group} (reference groups)")
+        g = accel(big, b, params(1, 0.01, 0.6), True)
+        g0 = accel(base, b, params(1, 0.01, 0.6), True)
+        assert np.isfinite(g.a).all()
+        assert rel_rms(g.a, ref_a) <= 1e-3
+        ok, c = big.body_costs()
+        assert ok and float(c.astype(np.float64).sum()) == float(g.times.interactions)
+        assert g.times.interactions > g0.times.interactions
+    finally:
+        big.close()
+        base.close()
