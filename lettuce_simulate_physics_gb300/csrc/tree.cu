@@ -1181,6 +1181,60 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
 // is the sequential one bit for bit while the per-child FP64 work runs in parallel.
 __device__ __forceinline__ double shfl8(double v, int src_lane) { return __shfl_sync(0xffffffffu, v, src_lane); }
 
+// One node per thread: the thread forms each child's terms and adds them in child order (the same
+// operations as the eight-lane form below, done once each). Used for levels with many nodes, where
+// FP64 throughput, not latency, bounds the level.
+__device__ void combine_node_serial(uint32_t p, uint32_t T, const uint4* __restrict__ nd_range,
+                                    const float4* __restrict__ nd_geo, Moments mo, float inv_theta,
+                                    const float* __restrict__ inv_theta_sys, const uint32_t* __restrict__ sys,
+                                    unsigned* err) {
+    if (p >= T) {
+        atomicOr(err, kErrNodeOverflow);
+        return;
+    }
+    const uint4 r = nd_range[p];
+    if (r.w == 0 || r.w > 8 || r.z + r.w > T) {
+        atomicOr(err, kErrNodeOverflow);
+        return;
+    }
+    const int nch = static_cast<int>(r.w);
+    double M = 0, sx = 0, sy = 0, sz = 0;
+    for (int q = 0; q < nch; ++q) {
+        const float4 cm = mo.com[r.z + q];
+        const double m = cm.w;
+        M = DADD(M, m);
+        sx = DADD(sx, DMUL(m, static_cast<double>(cm.x)));
+        sy = DADD(sy, DMUL(m, static_cast<double>(cm.y)));
+        sz = DADD(sz, DMUL(m, static_cast<double>(cm.z)));
+    }
+    const float4 g = nd_geo[p];
+    const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
+                 cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
+    double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
+    for (int q = 0; q < nch; ++q) {
+        const uint32_t c = r.z + q;
+        const float4 cm = mo.com[c], a = mo.q0[c], e = mo.q1[c];
+        const double m = cm.w;
+        const double dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
+                     dz = DSUB(static_cast<double>(cm.z), cz);
+        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+        const double m3 = DMUL(m, 3.0);
+        qxx = DADD(qxx, DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2))));
+        qyy = DADD(qyy, DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2))));
+        qzz = DADD(qzz, DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2))));
+        qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy)));
+        qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz)));
+        qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz)));
+    }
+    store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g,
+                  inv_theta_sys ? inv_theta_sys[sys_of(sys, static_cast<int>(r.x))] : inv_theta);
+}
+
+#ifndef LG_COMBINE_SERIAL_MIN
+#define LG_COMBINE_SERIAL_MIN 4096
+#endif
+constexpr unsigned COMBINE_SERIAL_MIN = LG_COMBINE_SERIAL_MIN;  // nodes in a level for one node per thread
+
 __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth,
                                 uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
                                 const float4* __restrict__ nd_geo, Moments mo, float inv_theta,
@@ -1188,6 +1242,12 @@ __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const Up
                                 unsigned* err) {
     const uint32_t T = eff(Tdev, Tcap);
     const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
+    if (hi - lo >= COMBINE_SERIAL_MIN) {  // warp-uniform: the whole launch takes one form
+        const unsigned stride = gridDim.x * blockDim.x;
+        for (unsigned k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += stride)
+            combine_node_serial(dep_nodes[k], T, nd_range, nd_geo, mo, inv_theta, inv_theta_sys, sys, err);
+        return;
+    }
     const int lane = threadIdx.x & 31, sub = lane >> 3, j = lane & 7, base_lane = lane & ~7;
     const unsigned warps = (gridDim.x * blockDim.x) >> 5;
     const unsigned wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
