@@ -10,14 +10,16 @@
 //    The traversal stack lives in global memory (one slice per warp).
 //  - Evaluation in chunks: when the lists fill up, the warp converts the entries once to
 //    coordinates relative to the group's box centre o, (x_hi - o) + x_lo in FP32, into
-//    struct-of-arrays chunks in shared memory, and every lane evaluates them for its IPT i-bodies
-//    (IPT = ceil(group size / 32)): quadrupole cell terms (cuda_backend.cu:783-800 /
+//    struct-of-arrays chunks in shared memory (a flush's cells, then its bodies, in one shared
+//    buffer), and every lane evaluates them for its IPT i-bodies, small groups splitting the
+//    entries across lane partitions: quadrupole cell terms (cuda_backend.cu:783-800 /
 //    cpu_backend.cpp:858-871 math) and softened body terms. Two consecutive entries are loaded
 //    as one float2 and evaluated together with packed f32x2 instructions (one issue slot for two
 //    FP32 operations). Chunk sums are added to running sums kept in shared memory with Kahan
 //    compensation.
 // The interaction count per body is the list length minus its own entry; the reference CPU
-// backend counts that self entry, so its count exceeds this one by exactly N.
+// backend counts that self entry, so its count exceeds this one by exactly N. The own entry adds
+// nothing to the acceleration (d = 0) and is excluded from the potential by index.
 #include "engine.cuh"
 #include "walk_common.cuh"
 
