@@ -1,6 +1,6 @@
 """Benchmark of the GB300 engine on the reference's headline workload.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload disk1m|plummer16k|plummer65k]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload disk1m|plummer16k|plummer65k|plummer1m]
 
 Workload (default, disk1m): the plain Barnes-Hut step with quadrupoles, theta 0.6, leaf <= 16,
 N = 1e6 exponential disk (sech^2 vertical profile, scale height 0.1, R <= 10, disk mass 1, central
@@ -42,6 +42,9 @@ WORKLOADS = {
                        desc="direct summation, N=16384 Plummer (Henon units, r<10a), eps 0.01, dt 1e-3"),
     "plummer65k": dict(kind="plummer", n=65536, seed=2, eps=0.01, dt=1e-3, theta=0.6, method="direct",
                        desc="direct summation, N=65536 Plummer (Henon units, r<10a), eps 0.01, dt 1e-3"),
+    "plummer1m": dict(kind="plummer", n=1_000_000, seed=1, eps=0.01, dt=1.0 / 128, theta=0.6, method="tree",
+                      desc="BH quadrupole tree, theta 0.6, N=1e6 Plummer (Henon units, r<10a), eps 0.01, dt 1/128 "
+                           "(the reference's published GPU configuration)"),
 }
 
 
