@@ -21,7 +21,18 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_cpu.so")
-DEFAULT_REF_SRC = "/root/reference/src"
+# The reference's sources: LETTUCE_REF_SRC (its src/), or LETTUCE_REF (a checkout), else the staged
+# copy that baseline/stage.py makes (git-ignored).
+STAGED_REF_SRC = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "lettuce", "src")
+
+
+def reference_src() -> str:
+    if os.environ.get("LETTUCE_REF_SRC"):
+        return os.environ["LETTUCE_REF_SRC"]
+    if os.environ.get("LETTUCE_REF"):
+        return os.path.join(os.environ["LETTUCE_REF"], "src")
+    return STAGED_REF_SRC
+
 
 NODE_DTYPE = np.dtype([("cx", "<f4"), ("cy", "<f4"), ("cz", "<f4"), ("m", "<f4"), ("qxx", "<f4"), ("qxy", "<f4"),
                        ("qxz", "<f4"), ("qyy", "<f4"), ("qyz", "<f4"), ("qzz", "<f4"), ("rcrit2", "<f4"),
@@ -38,7 +49,7 @@ def build(ref_src: str | None = None, quiet: bool = True) -> None:
     """Builds the port; also the reference library when its sources are present."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True, stdout=out)
-    src = ref_src or os.environ.get("LETTUCE_REF_SRC", DEFAULT_REF_SRC)
+    src = ref_src or reference_src()
     if os.path.isfile(os.path.join(src, "cpu_backend.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"], check=True, stdout=out)
 

@@ -91,6 +91,9 @@ def main():
     b = S.plummer(4096, 1, cut=20)
     save("direct_plummer4096", b, dict(G=G, eps=0.01),
          nopot=force_case(b, O.DIRECT, G, 0.01, 0.6, False), pot=force_case(b, O.DIRECT, G, 0.01, 0.6, True))
+    # Direct at the benchmark's direct workload: Plummer N = 16384, seed 1, r < 10a, eps 0.01.
+    b = S.plummer(16384, 1, cut=10)
+    save("direct_plummer16384", b, dict(G=G, eps=0.01), pot=force_case(b, O.DIRECT, G, 0.01, 0.6, True))
     # Tree, Plummer 8192, theta 0.6 and 0.
     b = S.plummer(8192, 3, cut=20)
     save("tree_plummer8192", b, dict(G=G, eps=0.01),

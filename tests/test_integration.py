@@ -1,21 +1,22 @@
 """The drop-in boundary from the reference's side: the reference's own drivers and test binary
 link against the C++ Backend adapter (integration/gb300_backend.cpp) and the engine library in
-place of src/cuda_backend.cu. CPU only; needs the reference sources (skipped where absent). Without
-a device the reference's CUDA tests SKIP through make_cuda_backend returning nullptr with a reason,
-which this checks too."""
+place of src/cuda_backend.cu. CPU only; needs the reference sources (LETTUCE_REF, or the staged copy
+made by baseline/stage.py; skipped where absent). Without a device the reference's CUDA tests SKIP
+through make_cuda_backend returning nullptr with a reason, which this checks too. The same binaries
+run on the GPU in tests/test_gpu_reference_suite.py."""
 import os
 import subprocess
 
 import pytest
 
+from baseline.stage import staged_root
 from lettuce_simulate_physics_gb300 import build as B
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("LETTUCE_REF", "/root/reference")
+REF = staged_root()
 INTEG = os.path.join(ROOT, "lettuce_simulate_physics_gb300", "integration")
 
-pytestmark = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "src", "backend.hpp")),
-                                reason="reference sources not present")
+pytestmark = pytest.mark.skipif(REF is None, reason="reference sources not present")
 
 
 @pytest.fixture(scope="module")
