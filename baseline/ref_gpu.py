@@ -119,7 +119,7 @@ def run(workload: str, steps: int, warmup: int, device: int = 0) -> dict:
     be.upload(z)
     be.compute_forces(method, G, eps, theta)
     be.kick(1.0)
-    (x, y, zz, vx, vy, vz, m, ids) = be.download()
+    (_, _, _, vx, vy, vz, _), ids = be.download()
     pos = np.stack([b.x, b.y, b.z], 1).astype(np.float64)
     acc = np.zeros((n, 3))
     acc[ids] = np.stack([vx, vy, vz], 1)

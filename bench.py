@@ -48,6 +48,15 @@ WORKLOADS = {
 }
 
 
+L2_NOTE = "flushed between timed steps (write of 2x L2 outside the step events)"
+
+
+def workload_config(w, n, world):
+    """The `config` object of both arms' lines (identical keys and values for the same workload)."""
+    return {"workload": w["desc"], "n": n, "method": w["method"], "theta": w["theta"],
+            "parallelism": "replicas" if world > 1 else "single-gpu", "l2": L2_NOTE}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -436,6 +445,122 @@ def collision_leg(L, local, n_each=8_000_000, steps=500, adj_steps=64, every=8, 
             "loss_radius": radius, "loss_width": width}
 
 
+def direct_leg(L, local, steps=20, warmup=3, cpu_steps=5, no_cpu=False):
+    """Direct summation at the plummer16k workload (N = 16384 Plummer, seed 1, r < 10a, eps 0.01,
+    dt 1e-3): device milliseconds per KDK step and per force call (CUDA events on the engine stream,
+    L2 flushed between steps outside the events), the direct kernel's roofline (20 flops per body
+    pair over the pair-loop time, against the FFMA throughput measured on the same GPU), and the
+    reference CPU algorithm on the host cores for the same step."""
+    w = WORKLOADS["plummer16k"]
+    b = make_bodies(w)
+    n = len(b)
+    be = L.CudaBackend(local)
+    p = L.ForceParams(G=1.0, eps=w["eps"], theta=w["theta"], method=L.ForceMethod.direct)
+    dt = w["dt"]
+
+    def step():
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        be.kick(0.5 * dt)
+
+    be.upload(b)
+    be.compute_forces(p, False)
+    for _ in range(max(warmup, 3)):
+        step()
+    be.synchronize()
+    step_ms, force_ms, pair_ms = [], [], []
+    for _ in range(steps):
+        be.flush_l2()
+        be.event_record(0)
+        step()
+        be.event_record(1)
+        step_ms.append(be.event_elapsed(0, 1))
+        t = be.times()
+        force_ms.append(t.force_ms)
+        pair_ms.append(t.walk_ms)
+    peak = be.probe_fp32_peak()
+    be.close()
+    flops = 20.0 * n * (n - 1)
+    achieved = statistics.fmean([flops / (t * 1e-3) / 1e12 for t in pair_ms])
+    out = {"workload": w["desc"], "n": n, "steps": steps, "ms_per_step": round(statistics.fmean(step_ms), 4),
+           "force_ms": round(statistics.fmean(force_ms), 4), "pair_loop_ms": round(statistics.fmean(pair_ms), 4),
+           "ginteractions_per_s": round(n * (n - 1) / (statistics.fmean(force_ms) * 1e-3) / 1e9, 1),
+           "roofline": {"bound": "fp32", "kernel": "direct", "achieved": round(achieved, 3), "peak": round(peak, 3),
+                        "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                        "peak_source": "measured FFMA throughput on this GPU (lg_probe_fp32_peak)",
+                        "flops_per_unit": {"body_pair": 20}}}
+    if not no_cpu:
+        cms, kind, threads = cpu_port_steps(b, w, cpu_steps)
+        out["cpu_baseline"] = {"value": round(cms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
+                               "sample": f"{cpu_steps} KDK steps of the full workload (N={n})"}
+        out["cpu_over_gpu"] = round(cms / out["ms_per_step"], 1)
+    return out
+
+
+def engine_bench_loop(L, local, w, steps=20, warmup=3):
+    """The engine timed exactly as baseline/ref_gpu.py times the reference's CUDA backend: the
+    reference's lettuce-bench step (kick, drift, compute_forces, kick, then times(), which waits
+    for the device), wall clock per step, no L2 flush; plus the engine's own phase split."""
+    b = make_bodies(w)
+    be = L.CudaBackend(local)
+    method = L.ForceMethod.tree if w["method"] == "tree" else L.ForceMethod.direct
+    p = L.ForceParams(G=1.0, eps=w["eps"], theta=w["theta"], method=method)
+    dt = w["dt"]
+
+    def step():
+        be.kick(0.5 * dt)
+        be.drift(dt)
+        be.compute_forces(p, False)
+        be.kick(0.5 * dt)
+        return be.times()
+
+    be.upload(b)
+    be.compute_forces(p, False)
+    err_med, err_max = force_error_sample(be, b, w)
+    for _ in range(max(warmup, 1)):
+        step()
+    wall, force, inter = [], [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        t = step()
+        wall.append((time.perf_counter() - t0) * 1e3)
+        force.append(t.force_ms)
+        inter.append(t.interactions)
+    be.close()
+    return {"ms_per_step_wall": round(statistics.fmean(wall), 4),
+            "median_ms_per_step_wall": round(statistics.median(wall), 4),
+            "force_ms": round(statistics.fmean(force), 4), "interactions_per_step": int(statistics.fmean(inter)),
+            "ginteractions_per_s": round(statistics.fmean(inter) / (statistics.fmean(force) * 1e-3) / 1e9, 2),
+            "force_error_vs_fp64": {"median": err_med, "p99": err_max, "sample_bodies": 256}}
+
+
+def reference_gpu_leg(L, local, names=("disk1m", "plummer1m"), steps=20, warmup=3):
+    """The reference's own CUDA backend (src/cuda_backend.cu built unmodified for sm_103a, see
+    baseline/) on the same GPU and the same bodies, against the engine timed the same way. The
+    reference runs in a child process (baseline/ref_gpu.py), so a failure there cannot disturb the
+    engine's measurements; its result, or its error, is reported."""
+    out = {}
+    for name in names:
+        w = WORKLOADS[name]
+        eng = engine_bench_loop(L, local, w, steps, warmup)
+        cmd = [sys.executable, os.path.join(ROOT, "baseline", "ref_gpu.py"), "--workload", name, "--steps",
+               str(steps), "--warmup", str(warmup), "--device", str(local)]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            ref = json.loads(lines[-1]) if r.returncode == 0 and lines else \
+                {"error": f"exit {r.returncode}: {(r.stderr or r.stdout)[-600:]}"}
+        except subprocess.TimeoutExpired:
+            ref = {"error": "timed out after 900 s"}
+        rec = {"workload": w["desc"], "reference": ref, "engine": eng}
+        if "ms_per_step_wall" in ref:
+            rec["speedup_step"] = round(ref["ms_per_step_wall"] / eng["ms_per_step_wall"], 3)
+            rec["speedup_force"] = round(ref["phases_ms"]["force"] / eng["force_ms"], 3)
+        out[name] = rec
+    return out
+
+
 def read_profile_traffic(workload):
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -478,7 +603,7 @@ def run_reference(args, w, world, rank, dist):
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": args.gpus,
         "steps": min(steps, args.ref_steps), "warmup": 1, "ms_per_step": round(ms, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f32-positions", "data": "synthetic (seeded)",
-        "config": {"workload": w["desc"], "n": w["n"], "method": w["method"], "theta": w["theta"]},
+        "config": workload_config(w, w["n"], world),
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
                          "sample": f"{min(steps, args.ref_steps)} KDK steps of the full workload (N={w['n']})"},
         "e2e": {"value": round(ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -624,8 +749,16 @@ def run_gb300(args, w, world, rank, local, dist):
     if rank == 0 and not args.no_ensemble:
         ens = ensemble_leg(L, local, steps=args.ensemble_steps, count=args.ensemble_count)
 
+    direct = None
+    if rank == 0 and not args.no_direct:
+        direct = direct_leg(L, local, no_cpu=args.no_cpu or world > 1)
+
+    refgpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        refgpu = reference_gpu_leg(L, local)
+
     coll = None
-    if rank == 0 and args.collision:
+    if rank == 0 and not args.no_collision:
         coll = collision_leg(L, local, n_each=args.collision_n, steps=args.collision_steps,
                              adj_steps=args.collision_adj_steps, every=args.collision_every)
 
@@ -634,9 +767,7 @@ def run_gb300(args, w, world, rank, local, dist):
             "metric": METRIC, "value": round(ms, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f64-positions", "data": "synthetic (seeded)",
-            "config": {"workload": w["desc"], "n": n, "method": w["method"], "theta": w["theta"],
-                       "parallelism": "replicas" if world > 1 else "single-gpu",
-                       "l2": "flushed between timed steps (write of 2x L2 outside the step events)"},
+            "config": workload_config(w, n, world),
             "phases_ms": {"sort": round(statistics.fmean(sort_ms), 4), "build": round(statistics.fmean(build_ms), 4),
                           "walk": round(statistics.fmean(walk_ms), 4), "force": round(statistics.fmean(force_ms), 4)},
             "interactions_per_step": int(statistics.fmean(inter)),
@@ -650,6 +781,8 @@ def run_gb300(args, w, world, rank, local, dist):
                          "peak_source": "measured FFMA throughput on this GPU (lg_probe_fp32_peak)",
                          "flops_per_unit": {"body_pair": 20, "cell_term": 65}},
             "cpu_baseline": cpu,
+            "direct_c0": direct,
+            "reference_gpu": refgpu,
             "adjoint": adj,
             "ensemble": ens,
             "collision": coll,
@@ -677,14 +810,17 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=1000, help="KDK steps of the adjoint leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--ensemble-steps", type=int, default=200, help="KDK steps of the ensemble leg")
-    ap.add_argument("--collision", action="store_true", help="run the two-disk collision leg (adjoint window)")
+    ap.add_argument("--no-collision", action="store_true", help="skip the two-disk collision leg (adjoint window)")
+    ap.add_argument("--no-direct", action="store_true", help="skip the direct-summation (plummer16k) leg")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference CUDA backend on the same GPU (disk1m and plummer1m)")
     ap.add_argument("--collision-n", type=int, default=8_000_000, help="bodies per disk of the collision leg")
     ap.add_argument("--collision-steps", type=int, default=500, help="KDK steps of the collision leg")
     ap.add_argument("--collision-adj-steps", type=int, default=64, help="adjoint window of the collision leg")
     ap.add_argument("--collision-every", type=int, default=8, help="checkpoint interval of the collision window")
     ap.add_argument("--adjoint-n", type=int, default=65536, help="bodies of the adjoint leg")
     ap.add_argument("--ensemble-count", type=int, default=512, help="systems of the ensemble leg")
-    ap.add_argument("--only", choices=["adjoint", "ensemble", "collision"],
+    ap.add_argument("--only", choices=["adjoint", "ensemble", "collision", "direct", "reference_gpu"],
                     help="run one leg alone (single GPU) and print its JSON result")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
@@ -696,6 +832,10 @@ def main():
             out = adjoint_leg(L, 0, steps=args.adjoint_steps, n=args.adjoint_n)
         elif args.only == "ensemble":
             out = ensemble_leg(L, 0, steps=args.ensemble_steps, count=args.ensemble_count)
+        elif args.only == "direct":
+            out = direct_leg(L, 0, no_cpu=args.no_cpu)
+        elif args.only == "reference_gpu":
+            out = reference_gpu_leg(L, 0)
         else:
             out = collision_leg(L, 0, n_each=args.collision_n, steps=args.collision_steps,
                                 adj_steps=args.collision_adj_steps, every=args.collision_every)

@@ -318,15 +318,18 @@ lg_status lg_ensemble_get_stats(lg_ensemble* en, lg_ensemble_stats* out);
 /* Direct-summation forces with no device allocation. No counterpart in the reference: it is for
  * callers that cannot allocate device memory when they need forces, such as a code that owns all
  * device memory through its own fixed arena, or a stepping loop that must avoid cudaMalloc's
- * implicit device synchronisation. The caller passes device arrays: posm[n] float4 (x, y, z, m)
- * and poslo[n] float4 (low parts of FP64 positions, or zeros), and receives acc[n] float4
- * (ax, ay, az, phi; phi only with potential != 0) on its stream (a cudaStream_t, NULL for the
- * legacy stream). The call synchronises that stream before it returns.
+ * implicit device synchronisation. The caller passes device arrays of the current device, each
+ * 16-byte aligned: posm[n] float4 (x, y, z, m) and poslo[n] float4 (low parts of FP64 positions,
+ * x - (double)(float)x, or zeros), and receives acc[n] float4 (ax, ay, az, phi; phi only with
+ * potential != 0) on its stream (a cudaStream_t, NULL for the legacy stream). Pointers that are
+ * misaligned or not device memory of the current device are rejected with LG_ERR_ARG before any
+ * work is enqueued. The call synchronises that stream before it returns.
  * Scratch is a static device array inside this library (16 MiB of split-j partial sums plus a
  * status word), held by every GPU that loads the library until the process exits; n above
- * 1,048,576 is rejected with LG_ERR_ARG. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress, which loads the module): make that first call before any stream
- * capture. All calls share the array and it keeps the last call's contents, so calls that
+ * 1,048,576 is rejected with LG_ERR_ARG. Each call looks up the array's device address in the
+ * current context (cudaGetSymbolAddress), so a context that was reset and recreated gets the new
+ * address; the first call on a device also loads the module, so make that first call before any
+ * stream capture. All calls share the array and it keeps the last call's contents, so calls that
  * overlap on the GPU (other streams, other host threads) race and must not be issued. */
 lg_status lg_direct_forces_noalloc(const void* posm, const void* poslo, int n, double G, double eps, int potential,
                                    void* acc, void* stream);

@@ -17,8 +17,10 @@
 // tiles that hold the block's own bodies). With eps == 0 the r2 > 0 guard drops self and
 // coincident pairs, as the reference does.
 #include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <type_traits>
-#include <mutex>
 
 #include "engine.cuh"
 
@@ -372,30 +374,38 @@ namespace {
 constexpr size_t kNoAllocStatusBytes = 256;
 constexpr size_t kNoAllocPartials = size_t(1) << 20;  // float4 entries (16 MiB)
 constexpr int kNoAllocMaxN = 1 << 20;
-constexpr int kNoAllocMaxDevices = 64;
 
 // Status words, then split-j partial sums. Part of the library image: every GPU that loads the
 // library holds these 16 MiB until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocStatusBytes + kNoAllocPartials * 16];
 
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};
-
-// Device address of g_noalloc_scratch for the current device, looked up once per device. The
-// host-side name is only a stand-in; kernels must be given this address.
-unsigned char* noalloc_scratch(int dev) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            fail(kRuntime, std::string("lg_direct_forces_noalloc: cudaGetSymbolAddress failed: ") +
-                               cudaGetErrorString(e));
-        }
-        g_noalloc_addr[dev] = p;
+// Device address of g_noalloc_scratch in the current context. The host-side name is only a
+// stand-in; kernels must be given this address. It is looked up on every call (a table lookup once
+// the module is loaded), so a context torn down and recreated (cudaDeviceReset) gets the new address.
+unsigned char* noalloc_scratch() {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(kRuntime, std::string("lg_direct_forces_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
     }
-    return static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return static_cast<unsigned char*>(p);
+}
+
+// The kernels stage positions with bulk copies, which need 16-byte-aligned global addresses on
+// this device: reject anything else on the host, before any launch.
+void noalloc_check_pointer(const void* p, const char* what, int dev) {
+    if (reinterpret_cast<uintptr_t>(p) & 15u)
+        fail(kArg, std::string("lg_direct_forces_noalloc: ") + what + " is not 16-byte aligned");
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(kArg, std::string("lg_direct_forces_noalloc: ") + what + " is not a CUDA pointer: " + cudaGetErrorString(e));
+    }
+    if ((a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) || a.device != dev)
+        fail(kArg, std::string("lg_direct_forces_noalloc: ") + what + " is not device memory of the current device " +
+                       std::to_string(dev));
 }
 
 }  // namespace
@@ -415,14 +425,27 @@ extern "C" lg_status lg_direct_forces_noalloc(const void* posm, const void* posl
         }
         int dev = 0;
         LG_CK(cudaGetDevice(&dev));
-        if (dev < 0 || dev >= lg::kNoAllocMaxDevices) lg::fail(lg::kArg, "lg_direct_forces_noalloc: device index too large");
+        lg::noalloc_check_pointer(posm, "posm", dev);
+        lg::noalloc_check_pointer(poslo, "poslo", dev);
+        lg::noalloc_check_pointer(acc, "acc", dev);
         int sms = 0;
         LG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        unsigned char* base = lg::noalloc_scratch(dev);
+        unsigned char* base = lg::noalloc_scratch();
         unsigned* err = reinterpret_cast<unsigned*>(base);
         float4* partial = reinterpret_cast<float4*>(base + lg::kNoAllocStatusBytes);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         lg::DirectShape sh = lg::default_direct_shape(n, sms);
+        // The engine's launch-shape override "ipt,slices" applies here too.
+        if (const char* d = std::getenv("LETTUCE_GB300_DIRECT")) {
+            int ipt = 0, slices = 0;
+            if (std::sscanf(d, "%d,%d", &ipt, &slices) != 2 || (ipt != 1 && ipt != 2 && ipt != 4 && ipt != 8) ||
+                slices < 1)
+                lg::fail(lg::kArg, std::string("LETTUCE_GB300_DIRECT must be 'ipt,slices' with ipt in {1,2,4,8}, not '") +
+                                       d + "'");
+            sh.ipt = ipt;
+            sh.slices = slices;
+        }
+        // Split-j partial sums beyond the static array's size: fewer slices.
         const long long cap = static_cast<long long>(lg::kNoAllocPartials) / n;
         if (sh.slices > cap) sh.slices = static_cast<int>(cap < 1 ? 1 : cap);
         lg::BodyArrays b;

@@ -241,9 +241,15 @@ void Engine::build_tree(const lg_force_params& p) {
     has_pe = false;
     acc_ok = false;
     LG_CK(cudaEventRecord(events[EV_BUILD0], stream));
-    tree_sort(*this);
+    {
+        NvtxRange r("lettuce sort");
+        tree_sort(*this);
+    }
     LG_CK(cudaEventRecord(events[EV_SORTED], stream));
-    tree_build(*this, p.theta);
+    {
+        NvtxRange r("lettuce build");
+        tree_build(*this, p.theta);
+    }
     LG_CK(cudaEventRecord(events[EV_BUILT], stream));
     tree_ok = true;
     pend_tree_times = true;
@@ -274,6 +280,7 @@ void Engine::compute_forces_with(const lg_force_params& p, bool potential, const
     const bool have_let = let.ntrees > 0;
     LG_CK(cudaEventRecord(events[EV_WALK0], stream));
     BodyArrays b = bodies(cur);
+    NvtxRange walk_range(tree_m ? "lettuce walk" : "lettuce direct");
     if (!tree_m) {
         DirectShape sh = direct_shape_override.ipt ? direct_shape_override : default_direct_shape(n, sms);
         int slices = std::max(1, sh.slices);
@@ -319,6 +326,7 @@ void Engine::kick(double dt) {
     LG_CK(cudaSetDevice(dev));
     if (n == 0) return;
     if (!acc_ok) fail(kLogic, "cuda kick: accelerations are stale (build_tree since the last force call)");
+    NvtxRange r("lettuce kick");
     LG_CK(cudaEventRecord(events[EV_KICK0], stream));
     launch_kick(bodies(cur), acc.as<float4>(), static_cast<float>(dt), n, stream);
     ++launches;
@@ -329,6 +337,7 @@ void Engine::kick(double dt) {
 void Engine::drift(double dt) {
     LG_CK(cudaSetDevice(dev));
     if (n == 0) return;
+    NvtxRange r("lettuce drift");
     LG_CK(cudaEventRecord(events[EV_DRIFT0], stream));
     launch_drift(bodies(cur), dt, n, stream);
     ++launches;

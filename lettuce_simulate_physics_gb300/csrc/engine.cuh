@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <memory>
 #include <string>
@@ -10,6 +11,15 @@
 #include "lg_engine.cuh"
 
 namespace lg {
+
+// NVTX range around the host-side enqueue of one phase (sort, build, walk, direct, kick, drift),
+// for timeline profilers; a no-op unless a profiler injects itself (nvtx3 is header-only).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct TreeState;     // tree.cu
 struct AdjointState;  // adjoint.cu
