@@ -7,7 +7,8 @@
 //    contains the group, or whose box distance d satisfies d^2 < rcrit2, is opened; an accepted
 //    leaf of <= 4 bodies is taken as bodies, other accepted nodes as cells; opened leaves give
 //    bodies, opened internal nodes push their children. Appends are warp-compacted with ballots.
-//    The traversal stack lives in global memory (one slice per warp).
+//    The traversal stack lives in shared memory as child blocks (one entry per opened node), with
+//    a global overflow slice per warp.
 //  - Evaluation in chunks: when the lists fill up, the warp converts the entries once to
 //    coordinates relative to the group's box centre o, (x_hi - o) + x_lo in FP32, into
 //    struct-of-arrays chunks in shared memory (a flush's cells, then its bodies, in one shared
@@ -70,6 +71,7 @@ struct __align__(16) WarpSmem {
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];
     uint32_t rpre[RL_CAP + 1];
+    uint32_t sstk[SSTK];  // traversal stack (shared part)
 };
 
 struct WalkArgs {

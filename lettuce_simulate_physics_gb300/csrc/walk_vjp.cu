@@ -70,6 +70,7 @@ struct __align__(16) VjpSmem {
     uint32_t clist[CL_CAP];
     uint2 rlist[RL_CAP];
     uint32_t rpre[RL_CAP + 1];
+    uint32_t sstk[SSTK];  // traversal stack (shared part)
 };
 
 struct VjpArgs {
