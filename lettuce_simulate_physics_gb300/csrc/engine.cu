@@ -73,6 +73,9 @@ Engine::Engine(int device) : dev(device) {
     name += walk_body ? ", per-body walk" : ", group walk " + std::to_string(group_max);
     if (!walk_body) name += walk_merge ? " (packed)" : " (reference groups)";
     LG_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    LG_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    LG_CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    LG_CK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
     for (auto& ev : events) LG_CK(cudaEventCreate(&ev));
     for (auto& ev : user_events) LG_CK(cudaEventCreate(&ev));
     small.reserve(4096);
@@ -87,12 +90,16 @@ Engine::Engine(int device) : dev(device) {
 Engine::~Engine() {
     cudaSetDevice(dev);
     if (stream) cudaStreamSynchronize(stream);
+    if (side) cudaStreamSynchronize(side);
     tree.reset();
     adjoint.reset();
     lets.reset();
     for (auto& ev : events) if (ev) cudaEventDestroy(ev);
     for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
     if (pinned_small) cudaFreeHost(pinned_small);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 

@@ -106,6 +106,10 @@ struct Engine {
     int l2_bytes = 0;
     std::string name;
     cudaStream_t stream = nullptr;
+    // Side stream for build work that overlaps the moment upsweep (group boxes), forked from and
+    // joined back into `stream` with the two events.
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     enum { EV_BUILD0, EV_SORTED, EV_BUILT, EV_WALK0, EV_WALK1, EV_KICK0, EV_KICK1, EV_DRIFT0, EV_DRIFT1, EV_COUNT };
     cudaEvent_t events[EV_COUNT] = {};
     static constexpr int kUserEvents = 16;

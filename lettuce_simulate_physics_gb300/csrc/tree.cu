@@ -23,9 +23,12 @@
 //     follow from binary searches over the sorted keys.
 //  6. Node indices of the reference (children contiguous, child blocks in parent pre-order):
 //     first child of v = 1 + exclusive scan of nchild over pre-order.
-//  7. Upsweep: one thread per leaf computes its FP64 moments, then climbs; at each parent the
-//     last-arriving child (atomic counter) combines all children in index order, so the result
-//     does not depend on arrival order.
+//  7. Upsweep in FP64, children always combined in index order: one launch for the leaves (one
+//     thread per leaf, leaves bucketed by body count), then one launch per depth from the deepest
+//     (four lanes per node, each sequential sum folded by one lane). The group boxes are computed
+//     on a side stream meanwhile. (A single-launch form in which the last-arriving child of each
+//     node combines it was measured slower: its combines run one node per thread in sparse warps,
+//     and an FP64 warp instruction costs the same however few lanes are active.)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -84,7 +87,7 @@ struct TreeState {
     // pre-order nodes
     DevBuf pn_lohi, pn_meta, pn_nchild, pn_cb, pn_cpu;
     // reference-order nodes
-    DevBuf nd_range, nd_com, nd_comlo, nd_q0, nd_q1, nd_geo, nd_parent, nd_arrive;
+    DevBuf nd_range, nd_com, nd_comlo, nd_q0, nd_q1, nd_geo, nd_parent;
     // groups
     DevBuf gflag, gidx, grp_node, grp_range, grp_box, leaf_cnt;
     // upsweep order
@@ -1176,83 +1179,32 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
 
 // Internal nodes of one depth: combine the children (already final) in index order, FP64, the
 // parallel-axis theorem for the traceless quadrupole (src/cpu_backend.cpp:642-663).
-// Eight lanes per node (four nodes per warp): lane j forms child j's terms, then every lane of the
-// node replays the reference's sequential child-order sums from the shuffled terms, so the result
-// is the sequential one bit for bit while the per-child FP64 work runs in parallel.
-__device__ __forceinline__ double shfl8(double v, int src_lane) { return __shfl_sync(0xffffffffu, v, src_lane); }
+// Four lanes per node, eight nodes per warp. Lane j forms the terms of children j and j + 4 (the
+// per-child FP64 work runs in parallel); each of the reference's sequential child-order sums is
+// then folded by one lane only, from terms shuffled in child order: M, sx, sy, sz by lanes 0..3;
+// qxx and qyy by lane 0, qzz and qxy by lane 1, qxz by lane 2, qyz by lane 3. Lanes 1..3 divide
+// their first sum by M together. Every FP64 operation of the reference is done once, in its order,
+// so the moments are the reference's bit for bit. (On this part an FP64 warp instruction holds a
+// scheduler's FP64 unit for about 64 cycles: the form keeps the number of FP64 warp instructions
+// per node low and spreads the nodes of a level over all schedulers.)
+__device__ __forceinline__ double shfl_d(double v, int src_lane) { return __shfl_sync(0xffffffffu, v, src_lane); }
 
-// One node per thread: the thread forms each child's terms and adds them in child order (the same
-// operations as the eight-lane form below, done once each). Used for levels with many nodes, where
-// FP64 throughput, not latency, bounds the level.
-__device__ void combine_node_serial(uint32_t p, uint32_t T, const uint4* __restrict__ nd_range,
-                                    const float4* __restrict__ nd_geo, Moments mo, float inv_theta,
-                                    const float* __restrict__ inv_theta_sys, const uint32_t* __restrict__ sys,
-                                    unsigned* err) {
-    if (p >= T) {
-        atomicOr(err, kErrNodeOverflow);
-        return;
-    }
-    const uint4 r = nd_range[p];
-    if (r.w == 0 || r.w > 8 || r.z + r.w > T) {
-        atomicOr(err, kErrNodeOverflow);
-        return;
-    }
-    const int nch = static_cast<int>(r.w);
-    double M = 0, sx = 0, sy = 0, sz = 0;
-    for (int q = 0; q < nch; ++q) {
-        const float4 cm = mo.com[r.z + q];
-        const double m = cm.w;
-        M = DADD(M, m);
-        sx = DADD(sx, DMUL(m, static_cast<double>(cm.x)));
-        sy = DADD(sy, DMUL(m, static_cast<double>(cm.y)));
-        sz = DADD(sz, DMUL(m, static_cast<double>(cm.z)));
-    }
-    const float4 g = nd_geo[p];
-    const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
-                 cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
-    double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
-    for (int q = 0; q < nch; ++q) {
-        const uint32_t c = r.z + q;
-        const float4 cm = mo.com[c], a = mo.q0[c], e = mo.q1[c];
-        const double m = cm.w;
-        const double dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
-                     dz = DSUB(static_cast<double>(cm.z), cz);
-        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
-        const double m3 = DMUL(m, 3.0);
-        qxx = DADD(qxx, DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2))));
-        qyy = DADD(qyy, DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2))));
-        qzz = DADD(qzz, DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2))));
-        qxy = DADD(qxy, DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy)));
-        qxz = DADD(qxz, DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz)));
-        qyz = DADD(qyz, DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz)));
-    }
-    store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g,
-                  inv_theta_sys ? inv_theta_sys[sys_of(sys, static_cast<int>(r.x))] : inv_theta);
-}
+constexpr int COMBINE_BS = 128;
+constexpr int COMBINE_NODES = COMBINE_BS / 4;  // nodes per block and round
 
-#ifndef LG_COMBINE_SERIAL_MIN
-#define LG_COMBINE_SERIAL_MIN 4096
-#endif
-constexpr unsigned COMBINE_SERIAL_MIN = LG_COMBINE_SERIAL_MIN;  // nodes in a level for one node per thread
-
-__global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const UpsweepIndex* ix, int depth,
-                                uint32_t Tcap, const unsigned* Tdev, const uint4* __restrict__ nd_range,
-                                const float4* __restrict__ nd_geo, Moments mo, float inv_theta,
-                                const float* __restrict__ inv_theta_sys, const uint32_t* __restrict__ sys,
-                                unsigned* err) {
+__global__ void __launch_bounds__(COMBINE_BS) k_combine_level(const uint32_t* __restrict__ dep_nodes,
+                                                              const UpsweepIndex* ix, int depth, uint32_t Tcap,
+                                                              const unsigned* Tdev, const uint4* __restrict__ nd_range,
+                                                              const float4* __restrict__ nd_geo, Moments mo,
+                                                              float inv_theta, const float* __restrict__ inv_theta_sys,
+                                                              const uint32_t* __restrict__ sys, unsigned* err) {
     const uint32_t T = eff(Tdev, Tcap);
     const unsigned lo = ix->dep_off[depth], hi = ix->dep_off[depth + 1];
-    if (hi - lo >= COMBINE_SERIAL_MIN) {  // warp-uniform: the whole launch takes one form
-        const unsigned stride = gridDim.x * blockDim.x;
-        for (unsigned k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += stride)
-            combine_node_serial(dep_nodes[k], T, nd_range, nd_geo, mo, inv_theta, inv_theta_sys, sys, err);
-        return;
-    }
-    const int lane = threadIdx.x & 31, sub = lane >> 3, j = lane & 7, base_lane = lane & ~7;
+    const int lane = threadIdx.x & 31, j = lane & 3, base = lane & ~3;
     const unsigned warps = (gridDim.x * blockDim.x) >> 5;
     const unsigned wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    for (unsigned k0 = lo + 4 * wid; k0 < hi; k0 += 4 * warps) {
-        const unsigned k = k0 + sub;
+    for (unsigned k0 = lo + 8 * wid; k0 < hi; k0 += 8 * warps) {  // warp-uniform
+        const unsigned k = k0 + static_cast<unsigned>(lane >> 2);
         bool valid = k < hi;
         uint32_t p = valid ? dep_nodes[k] : 0u;
         uint4 r = make_uint4(0, 0, 0, 0);
@@ -1269,57 +1221,76 @@ __global__ void k_combine_level(const uint32_t* __restrict__ dep_nodes, const Up
             }
         }
         const int nch = valid ? static_cast<int>(r.w) : 0;
-        const bool mine = j < nch;
-        float4 cm = make_float4(0, 0, 0, 0), a = cm, e = cm;
-        if (mine) {
-            const uint32_t c = r.z + j;
-            cm = mo.com[c];
-            a = mo.q0[c];
-            e = mo.q1[c];
+        // Terms of the lane's children c = j + 4 sl (zeros past the last child: never added).
+        double m[2], ccx[2], ccy[2], ccz[2], mx[2], my[2], mz[2];
+        float4 qa[2], qb[2];
+#pragma unroll
+        for (int sl = 0; sl < 2; ++sl) {
+            const int c = j + 4 * sl;
+            float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+            qa[sl] = cm;
+            qb[sl] = cm;
+            if (c < nch) {
+                cm = mo.com[r.z + c];
+                qa[sl] = mo.q0[r.z + c];
+                qb[sl] = mo.q1[r.z + c];
+            }
+            m[sl] = cm.w;
+            ccx[sl] = cm.x;
+            ccy[sl] = cm.y;
+            ccz[sl] = cm.z;
+            mx[sl] = DMUL(m[sl], ccx[sl]);
+            my[sl] = DMUL(m[sl], ccy[sl]);
+            mz[sl] = DMUL(m[sl], ccz[sl]);
         }
-        const double m = cm.w;
-        const double mx = DMUL(m, static_cast<double>(cm.x)), my = DMUL(m, static_cast<double>(cm.y)),
-                     mz = DMUL(m, static_cast<double>(cm.z));
-        double M = 0, sx = 0, sy = 0, sz = 0;
+        // Monopole sums in child order: lane j folds M (0), sx (1), sy (2), sz (3).
+        double f1 = 0;
+#pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const double tm = shfl8(m, base_lane + q), tx = shfl8(mx, base_lane + q), ty = shfl8(my, base_lane + q),
-                         tz = shfl8(mz, base_lane + q);
+            const int src = base + (q & 3), sl = q >> 2;
+            const double vm = shfl_d(m[sl], src), vx = shfl_d(mx[sl], src), vy = shfl_d(my[sl], src),
+                         vz = shfl_d(mz[sl], src);
+            const double v = j == 0 ? vm : j == 1 ? vx : j == 2 ? vy : vz;
+            if (q < nch) f1 = DADD(f1, v);
+        }
+        const double M = shfl_d(f1, base);
+        const float4 g = valid ? nd_geo[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float gj = j == 1 ? g.x : j == 2 ? g.y : g.z;
+        const double cj = M > 0 ? __ddiv_rn(f1, M) : static_cast<double>(gj);  // lane 0's is unused
+        const double cx = shfl_d(cj, base + 1), cy = shfl_d(cj, base + 2), cz = shfl_d(cj, base + 3);
+        // Quadrupole terms of the lane's children about the new centre.
+        double txx[2], tyy[2], tzz[2], txy[2], txz[2], tyz[2];
+#pragma unroll
+        for (int sl = 0; sl < 2; ++sl) {
+            const double dx = DSUB(ccx[sl], cx), dy = DSUB(ccy[sl], cy), dz = DSUB(ccz[sl], cz);
+            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+            const double m3 = DMUL(m[sl], 3.0);
+            txx[sl] = DADD(static_cast<double>(qa[sl].x), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
+            tyy[sl] = DADD(static_cast<double>(qa[sl].w), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
+            tzz[sl] = DADD(static_cast<double>(qb[sl].y), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
+            txy[sl] = DADD(static_cast<double>(qa[sl].y), DMUL(DMUL(m3, dx), dy));
+            txz[sl] = DADD(static_cast<double>(qa[sl].z), DMUL(DMUL(m3, dx), dz));
+            tyz[sl] = DADD(static_cast<double>(qb[sl].x), DMUL(DMUL(m3, dy), dz));
+        }
+        // Quadrupole sums in child order: lane 0 folds qxx and qyy, lane 1 qzz and qxy, lane 2 qxz,
+        // lane 3 qyz.
+        double fa = 0, fb = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int src = base + (q & 3), sl = q >> 2;
+            const double vxx = shfl_d(txx[sl], src), vyy = shfl_d(tyy[sl], src), vzz = shfl_d(tzz[sl], src),
+                         vxy = shfl_d(txy[sl], src), vxz = shfl_d(txz[sl], src), vyz = shfl_d(tyz[sl], src);
+            const double va = j == 0 ? vxx : j == 1 ? vzz : j == 2 ? vxz : vyz;
+            const double vb = j == 0 ? vyy : vxy;
             if (q < nch) {
-                M = DADD(M, tm);
-                sx = DADD(sx, tx);
-                sy = DADD(sy, ty);
-                sz = DADD(sz, tz);
+                fa = DADD(fa, va);
+                if (j < 2) fb = DADD(fb, vb);
             }
         }
-        const float4 g = valid ? nd_geo[p] : make_float4(0, 0, 0, 0);
-        const double cx = M > 0 ? __ddiv_rn(sx, M) : g.x, cy = M > 0 ? __ddiv_rn(sy, M) : g.y,
-                     cz = M > 0 ? __ddiv_rn(sz, M) : g.z;
-        const double dx = DSUB(static_cast<double>(cm.x), cx), dy = DSUB(static_cast<double>(cm.y), cy),
-                     dz = DSUB(static_cast<double>(cm.z), cz);
-        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
-        const double m3 = DMUL(m, 3.0);
-        const double txx = DADD(static_cast<double>(a.x), DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
-        const double tyy = DADD(static_cast<double>(a.w), DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
-        const double tzz = DADD(static_cast<double>(e.y), DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
-        const double txy = DADD(static_cast<double>(a.y), DMUL(DMUL(m3, dx), dy));
-        const double txz = DADD(static_cast<double>(a.z), DMUL(DMUL(m3, dx), dz));
-        const double tyz = DADD(static_cast<double>(e.x), DMUL(DMUL(m3, dy), dz));
-        double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
-        for (int q = 0; q < 8; ++q) {
-            const int sl = base_lane + q;
-            const double vxx = shfl8(txx, sl), vxy = shfl8(txy, sl), vxz = shfl8(txz, sl), vyy = shfl8(tyy, sl),
-                         vyz = shfl8(tyz, sl), vzz = shfl8(tzz, sl);
-            if (q < nch) {
-                qxx = DADD(qxx, vxx);
-                qyy = DADD(qyy, vyy);
-                qzz = DADD(qzz, vzz);
-                qxy = DADD(qxy, vxy);
-                qxz = DADD(qxz, vxz);
-                qyz = DADD(qyz, vyz);
-            }
-        }
+        const double qzz = shfl_d(fa, base + 1), qxy = shfl_d(fb, base + 1), qxz = shfl_d(fa, base + 2),
+                     qyz = shfl_d(fa, base + 3);
         if (valid && j == 0)
-            store_moments(mo, p, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g,
+            store_moments(mo, p, M, cx, cy, cz, fa, qxy, qxz, fb, qyz, qzz, g,
                           inv_theta_sys ? inv_theta_sys[sys_of(sys, static_cast<int>(r.x))] : inv_theta);
     }
 }
@@ -1628,11 +1599,20 @@ void tree_build(Engine& e, double theta) {
                                   t.nd_parent.as<uint32_t>(), t.leaf_node.as<uint32_t>(), t.gidx.as<uint32_t>(),
                                   t.grp_node.as<uint32_t>(), reinterpret_cast<int*>(counts + 4), e.err_word());
     LG_LAUNCHED();
-    k_groups<<<tb, BS, 0, s>>>(t.grp_node.as<uint32_t>(), t.pn_lohi.as<uint2>(), Tc, Tdev, e.bodies(e.cur), counts + 3,
-                               t.grp_range.as<uint2>(), t.grp_box.as<float4>());
-    LG_LAUNCHED();
-    e.launches += 3;
     t.merged = e.walk_merge && !sys;
+    // The group boxes do not depend on the moments: with the reference groups they are computed on
+    // the side stream while the FP64 upsweep runs, and joined back before the build returns.
+    cudaStream_t gs = s;
+    if (!t.merged) {
+        LG_CK(cudaEventRecord(e.fork_ev, s));
+        LG_CK(cudaStreamWaitEvent(e.side, e.fork_ev, 0));
+        gs = e.side;
+    }
+    k_groups<<<tb, BS, 0, gs>>>(t.grp_node.as<uint32_t>(), t.pn_lohi.as<uint2>(), Tc, Tdev, e.bodies(e.cur), counts + 3,
+                                t.grp_range.as<uint2>(), t.grp_box.as<float4>());
+    LG_LAUNCHED();
+    if (!t.merged) LG_CK(cudaEventRecord(e.join_ev, e.side));
+    e.launches += 3;
     if (t.merged) {
         t.mcount.reserve(T * 4 + 4);
         t.moff.reserve(T * 4 + 4);
@@ -1674,13 +1654,14 @@ void tree_build(Engine& e, double theta) {
         mo, inv_theta, t.inv_theta_sys, sys, e.err_word());
     LG_LAUNCHED();
     e.launches += 4;
-    const int cb = std::max(1, std::min(4 * e.sms, grid_for(static_cast<long long>(T), 128)));
+    const int cb = std::max(1, std::min(2 * e.sms, grid_for(static_cast<long long>(T), COMBINE_NODES)));
     for (int d = depth - 1; d >= 0; --d) {
-        k_combine_level<<<cb, 128, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, Tc, Tdev, t.nd_range.as<uint4>(),
+        k_combine_level<<<cb, COMBINE_BS, 0, s>>>(t.dep_nodes.as<uint32_t>(), ix, d, Tc, Tdev, t.nd_range.as<uint4>(),
                                            t.nd_geo.as<float4>(), mo, inv_theta, t.inv_theta_sys, sys, e.err_word());
         LG_LAUNCHED();
         ++e.launches;
     }
+    if (!t.merged) LG_CK(cudaStreamWaitEvent(s, e.join_ev, 0));
 }
 
 // After a synchronising point: true if the tree built with guessed sizes is valid (no key restart
@@ -1859,7 +1840,7 @@ size_t tree_held_bytes(const Engine& e) {
                             &t.runid, &t.bdepth, &t.flag, &t.leafid, &t.frame, &t.runs, &t.runcube, &t.counts,
                             &t.leaf_first, &t.leaf_depth, &t.leaf_c, &t.leaf_pre, &t.leaf_node, &t.pn_lohi,
                             &t.pn_meta, &t.pn_nchild, &t.pn_cb, &t.pn_cpu, &t.nd_range, &t.nd_com, &t.nd_comlo,
-                            &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.nd_arrive, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt, &t.ups, &t.dep_nodes, &t.leaf_order,
+                            &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt, &t.ups, &t.dep_nodes, &t.leaf_order,
                             &t.grp_range, &t.grp_box, &t.scan_state, &t.scan_ctr})
         h += d->capacity();
     return h;
