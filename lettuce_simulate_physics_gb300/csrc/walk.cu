@@ -52,9 +52,13 @@ constexpr int WARPS = WBS / 32;
 constexpr int CCH = LG_WALK_CCH;  // cells converted per chunk (a multiple of 8)
 constexpr int BCH = LG_WALK_BCH;  // bodies converted per chunk (a multiple of 8)
 static_assert(CCH % 8 == 0 && BCH % 8 == 0, "chunks hold whole pairs of every partition");
-constexpr int PASS = 128; // i-bodies per pass (4 per lane)
+#ifndef LG_WALK_IPT
+#define LG_WALK_IPT 4
+#endif
+constexpr int IPT_MAX = LG_WALK_IPT;  // i-bodies per lane at most
+static_assert(IPT_MAX >= 1 && IPT_MAX <= 4, "1 to 4 i-bodies per lane");
+constexpr int PASS = 32 * IPT_MAX;  // i-bodies per pass
 
-constexpr int IPT_MAX = 4;
 
 // Per-warp shared memory. Chunks are struct-of-arrays so that entries k, k+1 load as one float2.
 struct __align__(16) WarpSmem {
@@ -219,9 +223,9 @@ __device__ __forceinline__ void eval_cells_n(int ipt, WarpSmem& s, int cc, int k
                                              const float (&zi)[IPT_MAX], float e2) {
     switch (ipt) {
         case 1: eval_cells<1, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
-        case 2: eval_cells<2, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
-        case 3: eval_cells<3, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
-        default: eval_cells<4, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 2: eval_cells<(IPT_MAX < 2 ? IPT_MAX : 2), POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        case 3: eval_cells<(IPT_MAX < 3 ? IPT_MAX : 3), POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
+        default: eval_cells<IPT_MAX, POT, EPS0>(s, cc, k0, kstep, lane, xi, yi, zi, e2); break;
     }
 }
 
@@ -231,9 +235,9 @@ __device__ __forceinline__ void eval_bodies_n(int ipt, WarpSmem& s, int bc, int 
                                               const float (&zi)[IPT_MAX], const int (&kself)[IPT_MAX], float e2) {
     switch (ipt) {
         case 1: eval_bodies<1, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
-        case 2: eval_bodies<2, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
-        case 3: eval_bodies<3, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
-        default: eval_bodies<4, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        case 2: eval_bodies<(IPT_MAX < 2 ? IPT_MAX : 2), POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        case 3: eval_bodies<(IPT_MAX < 3 ? IPT_MAX : 3), POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
+        default: eval_bodies<IPT_MAX, POT, EPS0>(s, bc, k0, kstep, lane, xi, yi, zi, kself, e2); break;
     }
 }
 
