@@ -135,17 +135,17 @@ __device__ __forceinline__ uint64_t spread21(uint64_t v) {
 }
 
 // Quantised coordinate of src/cpu_backend.cpp:423: uint64(clamp((v - o) * s, 0, lim)), FP64,
-// round-to-nearest products, truncation.
-__device__ __forceinline__ uint64_t quantize(double v, double o, double s, double lim) {
-    double q = __dmul_rn(__dsub_rn(v, o), s);
-    q = fmin(fmax(q, 0.0), lim);
-    return static_cast<uint64_t>(__double2ull_rz(q));
+// round-to-nearest products, truncation. The clamp is taken after the conversion, in integers:
+// the truncating conversion saturates (negative values give 0), and lim = 2^21 - 1 is an integer,
+// so min(trunc(q), lim) equals trunc(clamp(q, 0, lim)) for every q, with two FP64 operations fewer.
+constexpr uint64_t QLIM = (1ull << MAX_LEVEL) - 1;
+__device__ __forceinline__ uint64_t quantize(double v, double o, double s) {
+    const uint64_t u = __double2ull_rz(__dmul_rn(__dsub_rn(v, o), s));
+    return u < QLIM ? u : QLIM;
 }
 
 __device__ __forceinline__ uint64_t morton(double x, double y, double z, double ox, double oy, double oz, double s) {
-    const double lim = static_cast<double>((1u << MAX_LEVEL) - 1);
-    return spread21(quantize(x, ox, s, lim)) << 2 | spread21(quantize(y, oy, s, lim)) << 1 |
-           spread21(quantize(z, oz, s, lim));
+    return spread21(quantize(x, ox, s)) << 2 | spread21(quantize(y, oy, s)) << 1 | spread21(quantize(z, oz, s));
 }
 
 // Common octal prefix (0..21) of two 63-bit keys.
