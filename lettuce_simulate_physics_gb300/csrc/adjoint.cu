@@ -344,7 +344,7 @@ struct AdjointState {
     double dt = 0;
     lg_force_params p{};
     DevBuf ck_x, ck_y, ck_z, ck_vx, ck_vy, ck_vz, ck_m, ck_id;  // checkpoints, nck * n each
-    DevBuf seg_hm, seg_lo;                         // direct: one segment's positions, every * n float4
+    DevBuf seg_hm[2], seg_lo[2];                   // direct: two segments' positions, every * n float4 each
     DevBuf seg_x, seg_y, seg_z, seg_id;            // tree: one segment's sorted FP64 positions and ids
     DevBuf m_by_id, w_sorted, gbuf;                // tree: masses by id, weights in body order, VJP output
     DevBuf lx, ly, lz, lvx, lvy, lvz, lm, loss_terms, w, partial;
@@ -491,8 +491,10 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
         a.w_sorted.reserve(static_cast<size_t>(n) * 16);
         a.gbuf.reserve(static_cast<size_t>(n) * 32);
     } else {
-        a.seg_hm.reserve(seg_n * 16);
-        a.seg_lo.reserve(seg_n * 16);
+        for (int b = 0; b < 2; ++b) {
+            a.seg_hm[b].reserve(seg_n * 16);
+            a.seg_lo[b].reserve(seg_n * 16);
+        }
     }
     LG_CK(cudaMemcpyAsync(a.tx.as<double>(), tx, nb8, cudaMemcpyHostToDevice, s));
     LG_CK(cudaMemcpyAsync(a.ty.as<double>(), ty, nb8, cudaMemcpyHostToDevice, s));
@@ -544,11 +546,11 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     const float e2 = static_cast<float>(a.p.eps * a.p.eps);
     const bool eps0 = !(e2 >= 1.17549435e-38f);
     const double h = 0.5 * a.dt;
-    for (int seg = (a.steps - 1) / a.every; seg >= 0; --seg) {
+    // Recomputes segment seg (checkpoint restore, then the segment's positions; the forces at the
+    // segment's last position and the closing kick after them are skipped, so a segment of k steps
+    // costs k - 1 force evaluations). Direct: into segment buffer seg & 1.
+    auto recompute = [&](int seg) {
         const int s0 = seg * a.every, s1 = std::min(a.steps, s0 + a.every);
-        // Restore the checkpoint at s0 and recompute the segment's positions.
-        // Only positions are needed: the forces at the segment's last position (and the closing
-        // kick after them) are skipped, so a segment of k steps costs k - 1 force evaluations.
         restore_ck(e, a, seg);
         const bool more = s1 - s0 >= 2;
         if (tree) {
@@ -565,8 +567,10 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
                 store_step(e, a, st - s0 + 1);
             }
         } else {
+            float4* hm = a.seg_hm[seg & 1].as<float4>();
+            float4* lo = a.seg_lo[seg & 1].as<float4>();
             if (more) direct_forces(e, a.p);
-            k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>(), a.seg_lo.as<float4>(), n);
+            k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), hm, lo, n);
             LG_LAUNCHED();
             for (int st = s0; st < s1 - 1; ++st) {
                 launch_kick(e.bodies(e.cur), e.acc.as<float4>(), static_cast<float>(0.5 * a.dt), n, s);
@@ -578,17 +582,19 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
                     ++e.launches;
                 }
                 const size_t so = static_cast<size_t>(st - s0 + 1) * n;
-                k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
-                                               n);
+                k_copy_hilo<<<gb, 256, 0, s>>>(e.bodies(e.cur), hm + so, lo + so, n);
                 LG_LAUNCHED();
             }
             e.launches += 1 + (s1 - 1 - s0);
         }
-        // Reverse through the segment.
+    };
+    // Reverse sweep through segment seg on stream vs (direct: from segment buffer seg & 1).
+    auto sweep = [&](int seg, cudaStream_t vs) {
+        const int s0 = seg * a.every, s1 = std::min(a.steps, s0 + a.every);
         for (int st = s1 - 1; st >= s0; --st) {
             const double c = st > 0 ? a.dt : h;
-            k_adj_kick<<<gb, 256, 0, s>>>(a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
-                                          a.lvy.as<double>(), a.lvz.as<double>(), a.dt, c, a.w.as<float4>(), n);
+            k_adj_kick<<<gb, 256, 0, vs>>>(a.lx.as<double>(), a.ly.as<double>(), a.lz.as<double>(), a.lvx.as<double>(),
+                                           a.lvy.as<double>(), a.lvz.as<double>(), a.dt, c, a.w.as<float4>(), n);
             LG_LAUNCHED();
             const size_t so = static_cast<size_t>(st - s0) * n;
             if (tree) {
@@ -611,20 +617,59 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
                 LG_CK(cudaStreamSynchronize(s));
                 e.check_device_errors("adjoint backward (tree VJP)");
             } else {
+                const float4* hm = a.seg_hm[seg & 1].as<float4>() + so;
+                const float4* lo = a.seg_lo[seg & 1].as<float4>() + so;
                 dim3 grid(iblocks, slices);
                 if (eps0)
-                    k_vjp<true><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
-                                                     a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
+                    k_vjp<true><<<grid, VBS, 0, vs>>>(hm, lo, a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
                 else
-                    k_vjp<false><<<grid, VBS, 0, s>>>(a.seg_hm.as<float4>() + so, a.seg_lo.as<float4>() + so,
-                                                      a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
+                    k_vjp<false><<<grid, VBS, 0, vs>>>(hm, lo, a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());
                 LG_LAUNCHED();
-                k_vjp_apply<<<gb, 256, 0, s>>>(a.partial.as<float4>(), n, slices, a.p.G, a.lx.as<double>(),
-                                               a.ly.as<double>(), a.lz.as<double>(), a.lm.as<double>());
+                k_vjp_apply<<<gb, 256, 0, vs>>>(a.partial.as<float4>(), n, slices, a.p.G, a.lx.as<double>(),
+                                                a.ly.as<double>(), a.lz.as<double>(), a.lm.as<double>());
                 LG_LAUNCHED();
                 e.launches += 3;
             }
         }
+    };
+    const int last = (a.steps - 1) / a.every;
+    if (tree) {
+        // The tree VJP rebuilds trees through the engine: one stream, segment after segment.
+        for (int seg = last; seg >= 0; --seg) {
+            recompute(seg);
+            sweep(seg, s);
+        }
+    } else {
+        // Direct: the sweep of segment seg runs on the side stream while the main stream recomputes
+        // segment seg - 1 into the other buffer (the two are independent; the GPU takes both at
+        // once). A sweep waits for its segment's recompute; a recompute waits for the sweep that
+        // last read its buffer. The operations and their order per stream are unchanged, so the
+        // gradients are those of the one-stream sweep bit for bit.
+        cudaEvent_t ev[5];
+        for (auto& x : ev) LG_CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+        cudaEvent_t* rec_done = ev;        // [buffer]
+        cudaEvent_t* sweep_done = ev + 2;  // [buffer]
+        LG_CK(cudaEventRecord(ev[4], s));  // the adjoint state's initialisation
+        LG_CK(cudaStreamWaitEvent(e.side, ev[4], 0));
+        bool used[2] = {false, false};
+        recompute(last);
+        LG_CK(cudaEventRecord(rec_done[last & 1], s));
+        for (int seg = last; seg >= 0; --seg) {
+            LG_CK(cudaStreamWaitEvent(e.side, rec_done[seg & 1], 0));
+            sweep(seg, e.side);
+            LG_CK(cudaEventRecord(sweep_done[seg & 1], e.side));
+            used[seg & 1] = true;
+            if (seg > 0) {
+                const int b = (seg - 1) & 1;
+                if (used[b]) LG_CK(cudaStreamWaitEvent(s, sweep_done[b], 0));
+                recompute(seg - 1);
+                LG_CK(cudaEventRecord(rec_done[b], s));
+            }
+        }
+        LG_CK(cudaEventRecord(ev[4], e.side));
+        LG_CK(cudaStreamWaitEvent(s, ev[4], 0));
+        LG_CK(cudaStreamSynchronize(s));
+        for (auto& x : ev) cudaEventDestroy(x);
     }
     // Gradients in id order.
     std::vector<uint32_t> ids(static_cast<size_t>(n));
