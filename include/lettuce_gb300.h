@@ -10,8 +10,10 @@
  *    LG_ERR_RUNTIME is the reference's std::runtime_error, LG_ERR_LOGIC its std::logic_error
  *    (a call made in the wrong state, e.g. kick after build_tree without a force call).
  *  - Pointers are host pointers to plain arrays; sizes are element counts.
- *  - One engine = one device, one non-blocking stream. kick and drift are asynchronous; times,
- *    diagnostics, download, body_costs and the force calls synchronise, as in the reference.
+ *  - One engine = one device, one non-blocking stream (plus an internal second stream, forked from
+ *    and joined back into it, for work that overlaps inside one call: the group boxes of a tree
+ *    build, the adjoint's VJP sweep). kick and drift are asynchronous; times, diagnostics,
+ *    download, body_costs and the force calls synchronise, as in the reference.
  *  - Bodies cross the boundary as float32 (the reference's Bodies, src/bodies.hpp:7-10); inside,
  *    positions are FP64 and the drift is FP64. download() rounds positions to float.
  */
