@@ -13,7 +13,10 @@
 //     then one kernel per digit with decoupled look-back across tiles; digits that are constant
 //     over all keys are skipped on the device. Stable, so the permutation equals the reference's.
 //  3. Key restarts: runs of > 16 identical keys are re-keyed in their own bounding cube (the
-//     reference's rekey, src/cpu_backend.cpp:503-530) and sorted by (key, restart key).
+//     reference's rekey, src/cpu_backend.cpp:503-530) and sorted by the new keys inside each run;
+//     runs whose composite keys still tie are re-keyed again, up to FRAMES frames (depth 126).
+//     Composite keys (frame 0, then the restart frames) order the bodies as the reference's nested
+//     rekeys do, and a common-prefix length over them drives steps 4-6.
 //  4. Leaves from key windows: body i's leaf depth is 1 + the deepest common octal prefix of any
 //     window of LEAF_MAX+1 consecutive sorted keys that contains i (the first depth at which its
 //     cell holds <= LEAF_MAX bodies); group depth likewise with windows of group_max+1.
@@ -46,8 +49,20 @@ namespace {
 
 constexpr int LEAF_MAX = 16;   // src/cpu_backend.cpp:24
 constexpr int MAX_LEVEL = 21;  // :28
-constexpr int MAX_DEPTH = 2 * MAX_LEVEL;  // frame 0 plus one key restart
+constexpr int FRAMES = 6;                     // key frames: frame 0 and up to five key restarts
+constexpr int MAX_DEPTH = FRAMES * MAX_LEVEL;  // 126: depths fit the 8-bit depth fields
 constexpr int BS = 256;
+
+// Key restart frames, in device memory. Frame f >= 1 re-keys, in its own bounding cube, every run
+// of more than LEAF_MAX bodies whose keys in frames 0..f-1 are all equal (the reference's rekey at
+// level kMaxLevel of frame f-1, src/cpu_backend.cpp:536-544); its runs are sorted by the new keys.
+struct FrameTable {
+    const uint64_t* key[FRAMES];  // [f >= 1] frame-f keys by sorted position (0 outside its runs)
+    const int* runid[FRAMES];     // [f >= 1] the body's run in frame f, or -1
+    const double* cube[FRAMES];   // [f >= 1] per run: origin xyz, side (0: coincident), 2^21 / side
+    const uint8_t* nfr;           // per body: frames it has keys in (1 + its non-coincident restarts)
+    int nf;                       // frames in use
+};
 
 inline int grid_for(long long n, int bs) { return static_cast<int>((n + bs - 1) / bs); }
 
@@ -78,10 +93,12 @@ struct SortCtl {
 struct TreeState {
     // sort
     DevBuf keysA, keysB, valsA, valsB, hist, lookback, ctl;
-    // sorted keys (frame 0 and restart keys), per-body tree data
-    DevBuf skey, skey1, key1tmp, runid, bdepth, flag, leafid;
-    // frame and key-restart runs
-    DevBuf frame, runs, runcube, counts;
+    // sorted frame-0 keys, per-body tree data
+    DevBuf skey, bdepth, flag, leafid;
+    // frame, key-restart runs and frames (index 0 of the per-frame buffers unused)
+    DevBuf frame, runs, counts, key1tmp, nfr, ftab;
+    DevBuf fkey[FRAMES], frunid[FRAMES], fcube[FRAMES];
+    int nframes = 1;  // key frames of the last restarted build
     // leaves
     DevBuf leaf_first, leaf_depth, leaf_c, leaf_pre, leaf_node;
     // pre-order nodes
@@ -94,7 +111,7 @@ struct TreeState {
     DevBuf ups, dep_nodes, leaf_order;
     // scan state
     DevBuf scan_state, scan_ctr;
-    size_t K = 0, T = 0, ngroups = 0, nruns = 0;  // sizes the last build was launched with
+    size_t K = 0, T = 0, ngroups = 0;  // sizes the last build was launched with
     int max_depth = 0;
     bool restarted = false;
     int group_max = 128;
@@ -155,20 +172,33 @@ __device__ __forceinline__ int cpl21(uint64_t a, uint64_t b) { return (__clzll(a
 // bodies of different systems share no prefix (-1), so no leaf, node or group spans two systems.
 // Single-system builds pass null.
 
-// Common octal prefix (0..42) of composite keys (key, restart key); -1 across systems.
-__device__ __forceinline__ int cpl42(const uint32_t* sys, const uint64_t* k0, const uint64_t* k1, int i, int j) {
+// Common octal prefix over the restart frames 1..nf-1 of bodies whose frame-0 keys are equal:
+// 21 per equal frame, 21 nf when every frame is equal.
+__device__ __forceinline__ int cpl_frames(const FrameTable* ft, int i, int j) {
+    const int nf = ft->nf;
+    for (int f = 1; f < nf; ++f) {
+        const uint64_t a = ft->key[f][i], b = ft->key[f][j];
+        if (a != b) return MAX_LEVEL * f + cpl21(a, b);
+    }
+    return MAX_LEVEL * nf;
+}
+
+// Common octal prefix (0..126) of the composite keys (frame 0, then the restart frames) of bodies
+// i and j; -1 across systems. ft is null when no key restart was needed.
+__device__ __forceinline__ int cpl_key(const uint32_t* sys, const uint64_t* k0, const FrameTable* ft, int i, int j) {
     if (sys && sys[i] != sys[j]) return -1;
     const uint64_t a = k0[i], b = k0[j];
-    if (a != b || !k1) return cpl21(a, b);
-    return MAX_LEVEL + cpl21(k1[i], k1[j]);
+    if (a != b || !ft) return cpl21(a, b);
+    return cpl_frames(ft, i, j);
 }
 
 __device__ __forceinline__ uint32_t sys_of(const uint32_t* sys, int i) { return sys ? sys[i] : 0u; }
 
-// Octal digit of composite key at depth d (1-based).
-__device__ __forceinline__ int digit_at(const uint64_t* k0, const uint64_t* k1, int i, int d) {
-    if (d <= MAX_LEVEL) return static_cast<int>((k0[i] >> (3 * (MAX_LEVEL - d))) & 7);
-    return static_cast<int>((k1[i] >> (3 * (2 * MAX_LEVEL - d))) & 7);
+// Octal digit of the composite key at depth d (1-based): digit d - 21 f of frame f = (d - 1) / 21.
+__device__ __forceinline__ int digit_at(const uint64_t* k0, const FrameTable* ft, int i, int d) {
+    const int f = (d - 1) / MAX_LEVEL;
+    const uint64_t k = f == 0 ? k0[i] : ft->key[f][i];
+    return static_cast<int>((k >> (3 * (MAX_LEVEL * (f + 1) - d))) & 7);
 }
 
 // ---- frame and keys --------------------------------------------------------------------------
@@ -496,7 +526,7 @@ __global__ void k_permute(const BodyArrays src, BodyArrays dst, const uint64_t* 
     if (i >= n_total) return;
     // Bodies past the tree's range (the forest's direct systems) keep their place.
     const uint32_t j = i < n ? vals[i] : static_cast<uint32_t>(i);
-    if (i < n) skey[i] = key_src ? key_src[j] : keys[i];
+    if (i < n && skey) skey[i] = key_src ? key_src[j] : keys[i];
     if (i >= n) {
         dst.x[i] = src.x[i]; dst.y[i] = src.y[i]; dst.z[i] = src.z[i];
         dst.hm[i] = src.hm[i]; dst.lo[i] = src.lo[i];
@@ -616,19 +646,22 @@ __global__ void __launch_bounds__(SCAN_BS) k_scan(const uint32_t* __restrict__ i
 }
 
 // ---- key restarts ----------------------------------------------------------------------------
-// A run of identical frame-0 keys longer than LEAF_MAX: appended as (start, end).
-__global__ void k_find_runs(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ skey, int n, uint2* runs,
+// The runs of frame f: maximal ranges of more than LEAF_MAX bodies of one system whose keys in
+// frames 0..f-1 are all equal, among the bodies re-keyed in every earlier frame (nfr == f; all
+// bodies for f = 1, where nfr and ft are null): appended as (start, end). ft holds frames 0..f-1.
+__global__ void k_find_runs(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ skey,
+                            const FrameTable* ft, const uint8_t* __restrict__ nfr, int f, int n, uint2* runs,
                             unsigned* count, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i + LEAF_MAX >= n) return;
-    const uint64_t k = skey[i];
-    const uint32_t sy = sys_of(sys, i);
-    if (i > 0 && skey[i - 1] == k && sys_of(sys, i - 1) == sy) return;
-    if (skey[i + LEAF_MAX] != k || sys_of(sys, i + LEAF_MAX) != sy) return;
-    int lo = i + LEAF_MAX, hi = n;  // first index with a different (system, key)
+    if (nfr && nfr[i] != f) return;
+    const int full = MAX_LEVEL * f;
+    if (i > 0 && cpl_key(sys, skey, ft, i - 1, i) >= full) return;
+    if (cpl_key(sys, skey, ft, i, i + LEAF_MAX) < full) return;
+    int lo = i + LEAF_MAX, hi = n;  // first index with a different (system, composite key)
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (skey[mid] == k && sys_of(sys, mid) == sy) lo = mid + 1;
+        if (cpl_key(sys, skey, ft, i, mid) >= full) lo = mid + 1;
         else hi = mid;
     }
     const unsigned r = atomicAdd(count, 1u);
@@ -681,15 +714,34 @@ __global__ void k_run_cube(const BodyArrays b, const uint2* runs, double* cube) 
     }
 }
 
-// Restart keys for bodies of non-coincident runs (0 elsewhere); runid = run index or -1.
-__global__ void k_run_keys(const BodyArrays b, const uint2* runs, const double* cube, uint64_t* key1, int* runid) {
+// Frame-f keys of the bodies of non-coincident runs (0 elsewhere, from a fill); runid = the run's
+// index (-1 elsewhere, from a fill); nfr = f + 1 for the re-keyed bodies.
+__global__ void k_run_keys(const BodyArrays b, const uint2* runs, const double* cube, uint64_t* key1, int* runid,
+                           uint8_t* nfr, int f) {
     const uint2 r = runs[blockIdx.x];
     const double* c = cube + 5 * blockIdx.x;
+    const bool rekeyed = c[3] > 0;
     for (unsigned i = r.x + threadIdx.x; i < r.y; i += BS) {
         runid[i] = static_cast<int>(blockIdx.x);
-        key1[i] = c[3] > 0 ? morton(b.x[i], b.y[i], b.z[i], c[0], c[1], c[2], c[4]) : 0ull;
+        if (rekeyed) {
+            key1[i] = morton(b.x[i], b.y[i], b.z[i], c[0], c[1], c[2], c[4]);
+            nfr[i] = static_cast<uint8_t>(f + 1);
+        }
     }
 }
+
+// Second key of the stable (run, frame key) sort: the run's first position for bodies of a run,
+// the body's own position otherwise, so that every body stays inside its run.
+__global__ void k_seg_keys(const uint32_t* __restrict__ vals, const int* __restrict__ runid,
+                           const uint2* __restrict__ runs, uint64_t* __restrict__ keys, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = vals[i];
+    const int r = runid[j];
+    keys[i] = r >= 0 ? runs[r].x : j;
+}
+
+__global__ void k_put_table(FrameTable v, FrameTable* dst) { *dst = v; }
 
 __global__ void k_fill_u64(uint64_t* a, uint64_t v, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -703,16 +755,10 @@ __global__ void k_iota(uint32_t* a, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = static_cast<uint32_t>(i);
 }
-// keys[i] = src[vals[i]]: carries a key array through the permutation in vals.
-__global__ void k_gather_keys(const uint64_t* __restrict__ src, const uint32_t* __restrict__ vals,
-                              uint64_t* __restrict__ keys, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) keys[i] = src[vals[i]];
-}
 
 // ---- leaves ----------------------------------------------------------------------------------
-// Per body: leaf depth and group depth from window common prefixes; cap(i) = 21 inside a
-// coincident frame-0 run, 42 otherwise. bdepth packs (leaf depth, group depth) as bytes.
+// Per body: leaf depth and group depth from window common prefixes, capped at 21 times the frames
+// the body has keys in. bdepth packs (leaf depth, group depth) as bytes.
 // Each block handles DEPTH_BS bodies: it first forms, in shared memory, the common prefixes
 // c_w(j) = cpl(key j, key j+w) of every window start its bodies need (w = 16 and w = group_max),
 // then every thread takes the maxima over its windows from shared memory.
@@ -720,20 +766,19 @@ constexpr int DEPTH_BS = 256;
 constexpr int GMAX_LIMIT = 1024;
 
 __global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0,
-                                                         const uint64_t* __restrict__ k1,
-                                                         const int* __restrict__ runid, const double* __restrict__ cube,
-                                                         int n, int gmax, uint16_t* __restrict__ bdepth) {
+                                                         const FrameTable* ft, int n, int gmax,
+                                                         uint16_t* __restrict__ bdepth) {
     __shared__ int8_t c16[DEPTH_BS + LEAF_MAX];
     __shared__ int8_t cg[DEPTH_BS + GMAX_LIMIT];
     const int i0 = blockIdx.x * DEPTH_BS;
     // Window starts j in [i0 - w, i0 + DEPTH_BS): slot j - (i0 - w).
     for (int t = threadIdx.x; t < DEPTH_BS + LEAF_MAX; t += DEPTH_BS) {
         const int j = i0 - LEAF_MAX + t;
-        c16[t] = static_cast<int8_t>((j >= 0 && j + LEAF_MAX < n) ? cpl42(sys, k0, k1, j, j + LEAF_MAX) : -1);
+        c16[t] = static_cast<int8_t>((j >= 0 && j + LEAF_MAX < n) ? cpl_key(sys, k0, ft, j, j + LEAF_MAX) : -1);
     }
     for (int t = threadIdx.x; t < DEPTH_BS + gmax; t += DEPTH_BS) {
         const int j = i0 - gmax + t;
-        cg[t] = static_cast<int8_t>((j >= 0 && j + gmax < n) ? cpl42(sys, k0, k1, j, j + gmax) : -1);
+        cg[t] = static_cast<int8_t>((j >= 0 && j + gmax < n) ? cpl_key(sys, k0, ft, j, j + gmax) : -1);
     }
     __syncthreads();
     const int i = i0 + threadIdx.x;
@@ -741,9 +786,9 @@ __global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint32_t* __restr
     // Windows containing i start at j in [i - w, i], i.e. slots [threadIdx.x, threadIdx.x + w].
     int best = -1;
     for (int t = threadIdx.x; t <= threadIdx.x + LEAF_MAX; ++t) best = max(best, static_cast<int>(c16[t]));
-    int cap = MAX_DEPTH;
-    if (!k1) cap = MAX_LEVEL;
-    else if (runid[i] >= 0 && cube[5 * runid[i] + 3] == 0) cap = MAX_LEVEL;
+    // A body's keys end with the last frame it was re-keyed in: coincident bodies, and bodies of a
+    // run past the last frame, stay one leaf there.
+    const int cap = ft ? MAX_LEVEL * ft->nfr[i] : MAX_LEVEL;
     const int ld = min(best + 1, cap);
     int gbest = -1;
     for (int t = threadIdx.x; t <= threadIdx.x + gmax; ++t) gbest = max(gbest, static_cast<int>(cg[t]));
@@ -751,18 +796,18 @@ __global__ void __launch_bounds__(DEPTH_BS) k_body_depth(const uint32_t* __restr
     bdepth[i] = static_cast<uint16_t>(ld | (gd << 8));
 }
 
-__global__ void k_leaf_flags(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+__global__ void k_leaf_flags(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const FrameTable* ft,
                              const uint16_t* __restrict__ bdepth, int n, uint32_t* __restrict__ flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int d = bdepth[i] & 255;
     uint32_t f = 1;
-    if (i > 0 && (bdepth[i - 1] & 255) == d && cpl42(sys, k0, k1, i - 1, i) >= d) f = 0;
+    if (i > 0 && (bdepth[i - 1] & 255) == d && cpl_key(sys, k0, ft, i - 1, i) >= d) f = 0;
     flag[i] = f;
 }
 
 // leaf_first, leaf_depth, leaf_c, and the node count of each leaf (its owned ancestors + itself).
-__global__ void k_leaf_info(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const uint64_t* __restrict__ k1,
+__global__ void k_leaf_info(const uint32_t* __restrict__ sys, const uint64_t* __restrict__ k0, const FrameTable* ft,
                             const uint16_t* __restrict__ bdepth, const uint32_t* __restrict__ flag,
                             const uint32_t* __restrict__ lid, int n, uint32_t* leaf_first, uint8_t* leaf_depth,
                             int8_t* leaf_c, uint32_t* leaf_nodes, int* max_depth) {
@@ -771,7 +816,7 @@ __global__ void k_leaf_info(const uint32_t* __restrict__ sys, const uint64_t* __
     const uint32_t l = lid[i];
     const int d = bdepth[i] & 255;
     atomicMax(max_depth, d);
-    const int c = i == 0 ? -1 : cpl42(sys, k0, k1, i - 1, i);
+    const int c = i == 0 ? -1 : cpl_key(sys, k0, ft, i - 1, i);
     leaf_first[l] = static_cast<uint32_t>(i);
     leaf_depth[l] = static_cast<uint8_t>(d);
     leaf_c[l] = static_cast<int8_t>(c);
@@ -781,8 +826,8 @@ __global__ void k_leaf_info(const uint32_t* __restrict__ sys, const uint64_t* __
 // ---- nodes -----------------------------------------------------------------------------------
 struct NodeCtx {
     const uint32_t* sys;  // per-body system (forest) or null
-    const uint64_t* k0;
-    const uint64_t* k1;
+    const uint64_t* k0;          // sorted frame-0 keys
+    const FrameTable* ft;        // key restart frames, or null
     const uint32_t* leaf_first;  // K+1
     const uint8_t* leaf_depth;
     const int8_t* leaf_c;
@@ -809,7 +854,7 @@ __device__ __forceinline__ uint32_t range_end(const NodeCtx& c, uint32_t lo, int
     uint32_t a = lo + 1, b = static_cast<uint32_t>(c.n);
     while (a < b) {
         uint32_t mid = (a + b) >> 1;
-        if (cpl42(c.sys, c.k0, c.k1, lo, mid) >= d) a = mid + 1;
+        if (cpl_key(c.sys, c.k0, c.ft, lo, mid) >= d) a = mid + 1;
         else b = mid;
     }
     return a;
@@ -880,36 +925,36 @@ __global__ void k_cpu_index(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, cons
 }
 
 // Geometric centre (FP64, the reference's iterative halving, src/cpu_backend.cpp:575-582 and
-// 585-592) of the node at depth d containing body b; restart cube at depth 21 for restarted runs.
-__device__ void node_geo(const NodeCtx& c, const double* frame, const int* runid, const double* cube, uint32_t b,
-                         int d, double& gx, double& gy, double& gz, double& half) {
+// 585-592) of the node at depth d containing body b; at depth 21 f the node of a run re-keyed in
+// frame f takes that run's cube (src/cpu_backend.cpp:536-544).
+__device__ void node_geo(const NodeCtx& c, const double* frame, uint32_t b, int d, double& gx, double& gy, double& gz,
+                         double& half) {
     frame += 5 * sys_of(c.sys, static_cast<int>(b));
     half = 0.5 * frame[3];
     gx = __dadd_rn(frame[0], half);
     gy = __dadd_rn(frame[1], half);
     gz = __dadd_rn(frame[2], half);
     for (int l = 1; l <= d; ++l) {
-        const int o = digit_at(c.k0, c.k1, b, l);
+        const int o = digit_at(c.k0, c.ft, b, l);
         const double q = 0.5 * half;
         gx = __dadd_rn(gx, (o & 4) ? q : -q);
         gy = __dadd_rn(gy, (o & 2) ? q : -q);
         gz = __dadd_rn(gz, (o & 1) ? q : -q);
         half = q;
-        if (l == MAX_LEVEL && runid && runid[b] >= 0) {
-            const double* cb = cube + 5 * runid[b];
-            if (cb[3] > 0) {
-                half = 0.5 * cb[3];
-                gx = __dadd_rn(cb[0], half);
-                gy = __dadd_rn(cb[1], half);
-                gz = __dadd_rn(cb[2], half);
-            }
+        if (c.ft && l % MAX_LEVEL == 0 && l / MAX_LEVEL < c.ft->nfr[b]) {
+            const int f = l / MAX_LEVEL;
+            const double* cb = c.ft->cube[f] + 5 * c.ft->runid[f][b];
+            half = 0.5 * cb[3];
+            gx = __dadd_rn(cb[0], half);
+            gy = __dadd_rn(cb[1], half);
+            gz = __dadd_rn(cb[2], half);
         }
     }
 }
 
 __global__ void k_nodes_out(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, const uint2* pn_lohi, const uint16_t* pn_meta,
                             const uint32_t* pn_nchild, const uint32_t* pn_cb, const uint32_t* pn_cpu,
-                            const double* frame, const int* runid, const double* cube, uint4* nd_range,
+                            const double* frame, uint4* nd_range,
                             float4* nd_geo, uint32_t* nd_parent, uint32_t* leaf_node, const uint32_t* gidx,
                             uint32_t* grp_node, int* max_depth, unsigned* err) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -928,7 +973,7 @@ __global__ void k_nodes_out(NodeCtx c, uint32_t Tcap, const unsigned* Tdev, cons
     }
     nd_range[me] = make_uint4(r.x, r.y, first, leaf ? 0u : nch);
     double gx, gy, gz, half;
-    node_geo(c, frame, runid, cube, r.x, d, gx, gy, gz, half);
+    node_geo(c, frame, r.x, d, gx, gy, gz, half);
     nd_geo[me] = make_float4(static_cast<float>(gx), static_cast<float>(gy), static_cast<float>(gz),
                              static_cast<float>(half));
     if (v == 0) nd_parent[0] = 0xffffffffu;
@@ -1075,7 +1120,7 @@ __device__ void store_moments(Moments mo, uint32_t node, double M, double cx, do
 #define DSUB __dsub_rn
 
 // Upsweep bookkeeping: internal nodes bucketed by depth, leaves bucketed by body count.
-constexpr int NDEP = 48;   // depth buckets (depth <= 42)
+constexpr int NDEP = MAX_DEPTH + 2;  // depth buckets (depth <= MAX_DEPTH + 1 with headroom)
 constexpr int NLSZ = 18;   // leaf-size buckets: 1..16, then larger
 struct UpsweepIndex {
     unsigned dep_count[NDEP], dep_off[NDEP + 1], dep_cur[NDEP];
@@ -1382,7 +1427,7 @@ void tree_sort(Engine& e) {
     t.frame.reserve(static_cast<size_t>(std::max(t.nsys, 1)) * 5 * 8 + 64);
     t.counts.reserve(64);
     t.restarted = false;
-    t.nruns = 0;
+    t.nframes = 1;
     if (sys) {
         k_frame_sys<<<t.nsys, BS, 0, s>>>(e.bodies(e.cur), t.sys_off, t.frame.as<double>());
     } else {
@@ -1414,12 +1459,13 @@ void tree_sort(Engine& e) {
     ++e.launches;
     e.cur = other;
 
-    // Key restarts (src/cpu_backend.cpp:541-544): runs of identical keys longer than a leaf.
+    // Key restarts (src/cpu_backend.cpp:536-544): runs of identical keys longer than a leaf.
     unsigned* counts = t.counts.as<unsigned>();
     LG_CK(cudaMemsetAsync(counts, 0, 64, s));
-    const int run_cap = std::max(1, n / (LEAF_MAX + 1) + 1);
+    const int run_cap = std::max(1, n / (LEAF_MAX + 1) + 1);  // runs hold more than LEAF_MAX bodies each
     t.runs.reserve(static_cast<size_t>(run_cap) * 8);
-    k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(sys, t.skey.as<uint64_t>(), n, t.runs.as<uint2>(), counts, run_cap);
+    k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(sys, t.skey.as<uint64_t>(), nullptr, nullptr, 1, n, t.runs.as<uint2>(),
+                                               counts, run_cap);
     LG_LAUNCHED();
     ++e.launches;
     // Key restarts are rare: unless the last build needed them, assume none and let the check after
@@ -1428,55 +1474,71 @@ void tree_sort(Engine& e) {
     if (t.speculative) return;
     LG_CK(cudaMemcpyAsync(e.pinned_small, counts, 4, cudaMemcpyDeviceToHost, s));
     LG_CK(cudaStreamSynchronize(s));
-    const unsigned R = e.pinned_small[0];
+    // Runs are disjoint and longer than LEAF_MAX, so there are fewer than run_cap.
+    unsigned R = std::min(e.pinned_small[0], static_cast<unsigned>(run_cap));
     t.restart_mode = R > 0;
     if (R == 0) return;
-    t.nruns = R;
     t.restarted = true;
     ++t.generation;
-    BodyArrays b = e.bodies(e.cur);
-    t.runcube.reserve(static_cast<size_t>(R) * 5 * 8);
-    t.runid.reserve(static_cast<size_t>(n) * 4);
-    t.skey1.reserve(static_cast<size_t>(n) * 8 + 8);
     t.key1tmp.reserve(static_cast<size_t>(n) * 8 + 8);
+    t.nfr.reserve(static_cast<size_t>(n) + 8);
+    t.ftab.reserve(sizeof(FrameTable));
     uint64_t* key1 = t.key1tmp.as<uint64_t>();
-    k_fill_i32<<<grid_for(n, BS), BS, 0, s>>>(t.runid.as<int>(), -1, n);
-    LG_LAUNCHED();
-    k_fill_u64<<<grid_for(n, BS), BS, 0, s>>>(key1, 0ull, n);
-    LG_LAUNCHED();
-    k_run_cube<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.runcube.as<double>());
-    LG_LAUNCHED();
-    k_run_keys<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.runcube.as<double>(), key1, t.runid.as<int>());
-    LG_LAUNCHED();
-    e.launches += 4;
-    // Stable sort by (key, restart key): LSD on the restart key, then on the key. Runs are ranges of
-    // equal keys, so every body stays inside its run and runid (by position) stays valid.
-    LG_CK(cudaMemcpyAsync(t.keysA.as<uint64_t>(), key1, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToDevice, s));
-    k_iota<<<grid_for(n, BS), BS, 0, s>>>(t.valsA.as<uint32_t>(), n);
-    LG_LAUNCHED();
-    sort_pairs(e, t, n);
-    k_gather_keys<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), t.valsA.as<uint32_t>(), t.keysA.as<uint64_t>(), n);
-    LG_LAUNCHED();
-    e.launches += 2;
-    sort_pairs(e, t, n);
-    if (sys) {
-        // Equal keys of different systems must not interleave: systems on top.
-        k_sys_keys<<<grid_for(n, BS), BS, 0, s>>>(sys, t.valsA.as<uint32_t>(), t.keysA.as<uint64_t>(), n);
+    uint8_t* nfr = t.nfr.as<uint8_t>();
+    LG_CK(cudaMemsetAsync(nfr, 1, static_cast<size_t>(n), s));
+    FrameTable ft{};
+    ft.key[0] = t.skey.as<uint64_t>();
+    ft.nfr = nfr;
+    // Frame by frame: re-key the runs in their own cubes, then a stable sort by (run, new key), which
+    // keeps every body inside its run. Inside a run the earlier frames' keys, run indices and nfr
+    // are all equal, so only the bodies and the new keys move.
+    for (int f = 1; f < FRAMES && R > 0; ++f) {
+        BodyArrays b = e.bodies(e.cur);
+        t.fkey[f].reserve(static_cast<size_t>(n) * 8 + 8);
+        t.frunid[f].reserve(static_cast<size_t>(n) * 4 + 4);
+        t.fcube[f].reserve(static_cast<size_t>(R) * 5 * 8);
+        int* runid = t.frunid[f].as<int>();
+        k_fill_i32<<<grid_for(n, BS), BS, 0, s>>>(runid, -1, n);
         LG_LAUNCHED();
-        ++e.launches;
+        k_fill_u64<<<grid_for(n, BS), BS, 0, s>>>(key1, 0ull, n);
+        LG_LAUNCHED();
+        k_run_cube<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.fcube[f].as<double>());
+        LG_LAUNCHED();
+        k_run_keys<<<R, BS, 0, s>>>(b, t.runs.as<uint2>(), t.fcube[f].as<double>(), key1, runid, nfr, f);
+        LG_LAUNCHED();
+        LG_CK(cudaMemcpyAsync(t.keysA.as<uint64_t>(), key1, static_cast<size_t>(n) * 8, cudaMemcpyDeviceToDevice, s));
+        k_iota<<<grid_for(n, BS), BS, 0, s>>>(t.valsA.as<uint32_t>(), n);
+        LG_LAUNCHED();
         sort_pairs(e, t, n);
-        k_gather_keys<<<grid_for(n, BS), BS, 0, s>>>(t.skey.as<uint64_t>(), t.valsA.as<uint32_t>(),
-                                                     t.keysA.as<uint64_t>(), n);
+        k_seg_keys<<<grid_for(n, BS), BS, 0, s>>>(t.valsA.as<uint32_t>(), runid, t.runs.as<uint2>(),
+                                                  t.keysA.as<uint64_t>(), n);
+        LG_LAUNCHED();
+        sort_pairs(e, t, n);
+        const int other = e.cur ^ 1;
+        k_permute<<<grid_for(n_total, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
+                                                       t.valsA.as<uint32_t>(), nullptr, key1, t.fkey[f].as<uint64_t>(), n,
+                                                       nullptr, n_total);
+        LG_LAUNCHED();
+        e.cur = other;
+        ft.key[f] = t.fkey[f].as<uint64_t>();
+        ft.runid[f] = runid;
+        ft.cube[f] = t.fcube[f].as<double>();
+        ft.nf = f + 1;
+        t.nframes = f + 1;
+        k_put_table<<<1, 1, 0, s>>>(ft, t.ftab.as<FrameTable>());
+        LG_LAUNCHED();
+        e.launches += 8;
+        if (f + 1 == FRAMES) break;  // runs left now stay leaves at depth MAX_DEPTH
+        // The next frame's runs: bodies re-keyed in this frame whose composite keys still tie.
+        LG_CK(cudaMemsetAsync(counts + 6, 0, 4, s));
+        k_find_runs<<<grid_for(n, BS), BS, 0, s>>>(sys, t.skey.as<uint64_t>(), t.ftab.as<FrameTable>(), nfr, f + 1, n,
+                                                   t.runs.as<uint2>(), counts + 6, run_cap);
         LG_LAUNCHED();
         ++e.launches;
+        LG_CK(cudaMemcpyAsync(e.pinned_small, counts + 6, 4, cudaMemcpyDeviceToHost, s));
+        LG_CK(cudaStreamSynchronize(s));
+        R = std::min(e.pinned_small[0], static_cast<unsigned>(run_cap));
     }
-    other = e.cur ^ 1;
-    k_permute<<<grid_for(n_total, BS), BS, 0, s>>>(e.bodies(e.cur), e.bodies(other), t.keysA.as<uint64_t>(),
-                                                   t.valsA.as<uint32_t>(), t.skey.as<uint64_t>(), key1,
-                                                   t.skey1.as<uint64_t>(), n, nullptr, n_total);
-    LG_LAUNCHED();
-    ++e.launches;
-    e.cur = other;
 }
 
 void tree_build(Engine& e, double theta) {
@@ -1487,9 +1549,7 @@ void tree_build(Engine& e, double theta) {
     t.group_max = e.group_max;
     t.theta = theta;
     const uint64_t* k0 = t.skey.as<uint64_t>();
-    const uint64_t* k1 = t.restarted ? t.skey1.as<uint64_t>() : nullptr;
-    const int* runid = t.restarted ? t.runid.as<int>() : nullptr;
-    const double* cube = t.restarted ? t.runcube.as<double>() : nullptr;
+    const FrameTable* ft = t.restarted ? t.ftab.as<FrameTable>() : nullptr;
     unsigned* counts = t.counts.as<unsigned>();
     const unsigned* Kdev = counts + 1;
     const unsigned* Tdev = counts + 2;
@@ -1505,15 +1565,15 @@ void tree_build(Engine& e, double theta) {
     t.leaf_node.reserve(n1 * 4);
     const int gb = grid_for(n, BS);
     if (t.group_max > GMAX_LIMIT) fail(kRuntime, "cuda tree build: group size above 1024");
-    k_body_depth<<<grid_for(n, DEPTH_BS), DEPTH_BS, 0, s>>>(sys, k0, k1, runid, cube, n, t.group_max,
+    k_body_depth<<<grid_for(n, DEPTH_BS), DEPTH_BS, 0, s>>>(sys, k0, ft, n, t.group_max,
                                                             t.bdepth.as<uint16_t>());
     LG_LAUNCHED();
-    k_leaf_flags<<<gb, BS, 0, s>>>(sys, k0, k1, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
+    k_leaf_flags<<<gb, BS, 0, s>>>(sys, k0, ft, t.bdepth.as<uint16_t>(), n, t.flag.as<uint32_t>());
     LG_LAUNCHED();
     e.launches += 2;
     scan_u32(e, t, t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n, counts + 1);
     LG_CK(cudaMemsetAsync(t.leaf_cnt.as<char>(), 0, n1 * 4, s));
-    k_leaf_info<<<gb, BS, 0, s>>>(sys, k0, k1, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
+    k_leaf_info<<<gb, BS, 0, s>>>(sys, k0, ft, t.bdepth.as<uint16_t>(), t.flag.as<uint32_t>(), t.leafid.as<uint32_t>(), n,
                                   t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
                                   t.leaf_cnt.as<uint32_t>(), reinterpret_cast<int*>(counts + 4));
     LG_LAUNCHED();
@@ -1568,7 +1628,7 @@ void tree_build(Engine& e, double theta) {
     for (DevBuf* d : {&t.nd_range, &t.nd_com, &t.nd_comlo, &t.nd_q0, &t.nd_q1, &t.nd_geo}) d->reserve(T * 16);
     t.nd_parent.reserve(T * 4);
     const uint32_t Tc = static_cast<uint32_t>(T), Kc = static_cast<uint32_t>(K);
-    NodeCtx c{sys, k0, k1, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
+    NodeCtx c{sys, k0, ft, t.leaf_first.as<uint32_t>(), t.leaf_depth.as<uint8_t>(), t.leaf_c.as<int8_t>(),
               t.leaf_pre.as<uint32_t>(), t.leafid.as<uint32_t>(), t.bdepth.as<uint16_t>(), n, Kdev, Kc,
               static_cast<unsigned>(sys ? t.nsys : 1)};
     const int tb = grid_for(static_cast<long long>(T), BS);
@@ -1595,7 +1655,7 @@ void tree_build(Engine& e, double theta) {
     LG_LAUNCHED();
     k_nodes_out<<<tb, BS, 0, s>>>(c, Tc, Tdev, t.pn_lohi.as<uint2>(), t.pn_meta.as<uint16_t>(),
                                   t.pn_nchild.as<uint32_t>(), t.pn_cb.as<uint32_t>(), t.pn_cpu.as<uint32_t>(),
-                                  t.frame.as<double>(), runid, cube, t.nd_range.as<uint4>(), t.nd_geo.as<float4>(),
+                                  t.frame.as<double>(), t.nd_range.as<uint4>(), t.nd_geo.as<float4>(),
                                   t.nd_parent.as<uint32_t>(), t.leaf_node.as<uint32_t>(), t.gidx.as<uint32_t>(),
                                   t.grp_node.as<uint32_t>(), reinterpret_cast<int*>(counts + 4), e.err_word());
     LG_LAUNCHED();
@@ -1754,9 +1814,9 @@ void tree_counts(Engine& e, size_t* nodes, size_t* leaves, size_t* groups, int* 
     if (max_depth) *max_depth = static_cast<int>(e.pinned_small[4]);
 }
 
-// The reference's key array after a build (src/cpu_backend.cpp:884-906 key_): frame-0 keys, with the
-// restart keys in place inside re-keyed runs (rekey overwrites key_ there; coincident runs keep
-// their frame-0 keys).
+// The reference's key array after a build (src/cpu_backend.cpp:884-906 key_): each body's key in
+// the last frame it was re-keyed in (rekey overwrites key_ inside a run; a coincident run keeps
+// the keys it had).
 void tree_keys(Engine& e, uint64_t* keys, size_t n) {
     TreeState& t = *e.tree;
     if (!e.tree_ok) fail(kLogic, "tree introspection: call build_tree (tree method) first");
@@ -1765,15 +1825,16 @@ void tree_keys(Engine& e, uint64_t* keys, size_t n) {
     const size_t N = static_cast<size_t>(e.n);
     LG_CK(cudaMemcpyAsync(keys, t.skey.as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));
     if (t.restarted) {
-        std::vector<uint64_t> k1(N);
-        std::vector<int> rid(N);
-        std::vector<double> cube(t.nruns * 5);
-        LG_CK(cudaMemcpyAsync(k1.data(), t.skey1.as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));
-        LG_CK(cudaMemcpyAsync(rid.data(), t.runid.as<int>(), N * 4, cudaMemcpyDeviceToHost, e.stream));
-        LG_CK(cudaMemcpyAsync(cube.data(), t.runcube.as<double>(), cube.size() * 8, cudaMemcpyDeviceToHost, e.stream));
+        std::vector<uint8_t> nfr(N);
+        std::vector<std::vector<uint64_t>> fk(t.nframes);
+        LG_CK(cudaMemcpyAsync(nfr.data(), t.nfr.as<uint8_t>(), N, cudaMemcpyDeviceToHost, e.stream));
+        for (int f = 1; f < t.nframes; ++f) {
+            fk[f].resize(N);
+            LG_CK(cudaMemcpyAsync(fk[f].data(), t.fkey[f].as<uint64_t>(), N * 8, cudaMemcpyDeviceToHost, e.stream));
+        }
         LG_CK(cudaStreamSynchronize(e.stream));
         for (size_t i = 0; i < N; ++i)
-            if (rid[i] >= 0 && cube[5 * static_cast<size_t>(rid[i]) + 3] > 0) keys[i] = k1[i];
+            if (nfr[i] > 1) keys[i] = fk[nfr[i] - 1][i];
     }
     LG_CK(cudaStreamSynchronize(e.stream));
 }
@@ -1836,13 +1897,14 @@ lg_memory_estimate memory_need(uint64_t n, int method) {
 size_t tree_held_bytes(const Engine& e) {
     const TreeState& t = *e.tree;
     size_t h = 0;
-    for (const DevBuf* d : {&t.keysA, &t.keysB, &t.valsA, &t.valsB, &t.hist, &t.lookback, &t.ctl, &t.skey, &t.skey1, &t.key1tmp,
-                            &t.runid, &t.bdepth, &t.flag, &t.leafid, &t.frame, &t.runs, &t.runcube, &t.counts,
+    for (const DevBuf* d : {&t.keysA, &t.keysB, &t.valsA, &t.valsB, &t.hist, &t.lookback, &t.ctl, &t.skey, &t.key1tmp,
+                            &t.nfr, &t.ftab, &t.bdepth, &t.flag, &t.leafid, &t.frame, &t.runs, &t.counts,
                             &t.leaf_first, &t.leaf_depth, &t.leaf_c, &t.leaf_pre, &t.leaf_node, &t.pn_lohi,
                             &t.pn_meta, &t.pn_nchild, &t.pn_cb, &t.pn_cpu, &t.nd_range, &t.nd_com, &t.nd_comlo,
                             &t.nd_q0, &t.nd_q1, &t.nd_geo, &t.nd_parent, &t.gflag, &t.gidx, &t.grp_node, &t.leaf_cnt, &t.ups, &t.dep_nodes, &t.leaf_order,
                             &t.grp_range, &t.grp_box, &t.scan_state, &t.scan_ctr})
         h += d->capacity();
+    for (int f = 1; f < FRAMES; ++f) h += t.fkey[f].capacity() + t.frunid[f].capacity() + t.fcube[f].capacity();
     return h;
 }
 

@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import lettuce_simulate_physics_gb300 as L
+from gpu_util import deep_radial, traversal_stack_depth, zero_v
 from lettuce_simulate_physics_gb300 import scenarios as S
 from oracle import oracle as O
 
@@ -119,6 +120,38 @@ def test_tree_adjoint_theta0_equals_direct_adjoint(be, eps):
     assert abs(lt / ld - 1) <= 1e-6
     tol = 1e-5 if eps > 0 else 1e-3  # unsoftened close pairs amplify FP32 rounding differences
     assert _rel(gxt, gxd) <= tol and _rel(gvt, gvd) <= tol and _rel(gmt, gmd) <= tol
+
+
+def test_deep_tree_adjoint_theta0_equals_direct_adjoint(be):
+    """The VJP walk runs the forward walk's traversal, spill to the warp's global stack slice
+    included: on a 1e5-body, 43-level tree whose smallest groups hold ~290 child blocks (more than
+    the 256 shared entries), the theta = 0 tree adjoint must still be the pairwise adjoint. The mass
+    gradient comes from the force VJP alone, so a lost or repeated subtree shows there."""
+    b = deep_radial(100_000, 3, 12)
+    port = O.OracleBackend("port", 0)
+    port.upload(zero_v(b))
+    port.build_tree(O.TREE, 0.0)
+    cg = port.groups()
+    h = np.maximum(np.maximum(cg["hx"], cg["hy"]), cg["hz"])
+    deepest = traversal_stack_depth(port, np.argsort(h, kind="stable")[:16])
+    assert (deepest > 256).sum() >= 4, deepest
+    port.close()
+    G, eps, dt, steps, every = 1.0, 0.03, 1e-2, 2, 2
+    rng = np.random.Generator(np.random.PCG64(8))
+    xstar = b.pos64() + rng.normal(0, 1e-2, (len(b), 3))
+    out = []
+    for method in (L.ForceMethod.direct, L.ForceMethod.tree):
+        be.upload(b)
+        be.adjoint_forward(L.ForceParams(G=G, eps=eps, theta=0.0, method=method), dt, steps, every)
+        out.append(be.adjoint_backward(xstar))
+    (ld, gxd, gvd, gmd), (lt, gxt, gvt, gmt) = out
+    worst = float(np.max(np.abs(gmt - gmd) / (np.abs(gmd) + 1e-3 * np.abs(gmd).max())))
+    print(f"deep tree adjoint: gm rel {_rel(gmt, gmd):.3g} (worst body {worst:.3g}), "
+          f"gx rel {_rel(gxt, gxd):.3g}, gv rel {_rel(gvt, gvd):.3g}")
+    assert np.isfinite(gxt).all() and np.isfinite(gmt).all()
+    assert abs(lt / ld - 1) <= 1e-6
+    assert _rel(gxt, gxd) <= 1e-5 and _rel(gvt, gvd) <= 1e-5 and _rel(gmt, gmd) <= 1e-5
+    assert worst <= 2e-4
 
 
 def _engine_with_groups(mode):
