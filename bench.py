@@ -494,7 +494,7 @@ def direct_leg(L, local, steps=20, warmup=3, cpu_steps=5, no_cpu=False):
                         "peak_source": "measured FFMA throughput on this GPU (lg_probe_fp32_peak)",
                         "flops_per_unit": {"body_pair": 20}}}
     if not no_cpu:
-        cms, kind, threads = cpu_port_steps(b, w, cpu_steps)
+        cms, kind, threads, _ = cpu_port_steps(b, w, cpu_steps)
         out["cpu_baseline"] = {"value": round(cms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
                                "sample": f"{cpu_steps} KDK steps of the full workload (N={n})"}
         out["cpu_over_gpu"] = round(cms / out["ms_per_step"], 1)
@@ -573,26 +573,38 @@ def read_profile_traffic(workload):
         return None
 
 
-def cpu_port_steps(b, w, steps, threads=0):
-    """The reference CPU algorithm (oracle/_ref if built from the reference, else the port):
-    `steps` KDK steps after one warm-up force call; returns (ms/step, kind, threads)."""
+def cpu_port_steps(b, w, steps, threads=0, warmup=0, budget_s=None):
+    """The reference CPU algorithm (oracle/_ref if built from the reference, else the port): one
+    force call, `warmup` untimed KDK steps, then up to `steps` timed KDK steps; with a budget, the
+    timed steps stop once they have used budget_s seconds (at least one runs). Returns (ms/step,
+    kind, threads, timed steps)."""
     from oracle import oracle as O
     O.build()
     kind = "ref" if O.available("ref") else "port"
     cpu = O.OracleBackend(kind, threads)
     method = O.TREE if w["method"] == "tree" else O.DIRECT
-    cpu.upload(b)
-    cpu.compute_forces(method, 1.0, w["eps"], w["theta"], False)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+
+    def step():
         cpu.kick(0.5 * w["dt"])
         cpu.drift(w["dt"])
         cpu.compute_forces(method, 1.0, w["eps"], w["theta"], False)
         cpu.kick(0.5 * w["dt"])
-    ms = (time.perf_counter() - t0) * 1e3 / max(steps, 1)
+
+    cpu.upload(b)
+    cpu.compute_forces(method, 1.0, w["eps"], w["theta"], False)
+    for _ in range(warmup):
+        step()
+    done = 0
+    t0 = time.perf_counter()
+    while done < max(steps, 1):
+        step()
+        done += 1
+        if budget_s is not None and time.perf_counter() - t0 >= budget_s:
+            break
+    ms = (time.perf_counter() - t0) * 1e3 / done
     nt = cpu.threads()
     cpu.close()
-    return ms, ("reference" if kind == "ref" else "port"), int(nt)
+    return ms, ("reference" if kind == "ref" else "port"), int(nt), done
 
 
 def run_reference(args, w, world, rank, dist):
@@ -600,15 +612,17 @@ def run_reference(args, w, world, rank, dist):
         return 0
     b = make_bodies(w)
     steps = max(1, args.steps)
-    # Bounded sample: the full-N step, as many as the budget allows (at least one).
-    ms, kind, threads = cpu_port_steps(b, w, min(steps, args.ref_steps))
+    # The full-N step, W untimed and K timed like the GPU arm; the timed steps stop early only if
+    # they exceed the time budget (a few minutes in all).
+    ms, kind, threads, done = cpu_port_steps(b, w, steps, warmup=max(0, args.warmup), budget_s=args.ref_budget_s)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/step", "n_gpus": args.gpus,
-        "steps": min(steps, args.ref_steps), "warmup": 1, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "steps": done, "warmup": max(0, args.warmup), "ms_per_step": round(ms, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-pairs/f32-positions", "data": "synthetic (seeded)",
         "config": workload_config(w, w["n"], world),
         "cpu_baseline": {"value": round(ms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
-                         "sample": f"{min(steps, args.ref_steps)} KDK steps of the full workload (N={w['n']})"},
+                         "sample": f"{done} timed KDK steps of the full workload (N={w['n']}) after one force call "
+                                   f"and {max(0, args.warmup)} untimed steps"},
         "e2e": {"value": round(ms, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -740,7 +754,7 @@ def run_gb300(args, w, world, rank, local, dist):
     # CPU baseline (rank 0, N=1): the reference CPU algorithm on this host's cores, bounded sample.
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cms, kind, threads = cpu_port_steps(b, w, args.ref_steps)
+        cms, kind, threads, _ = cpu_port_steps(b, w, args.ref_steps)
         cpu = {"value": round(cms, 3), "unit": "ms/step", "cores": threads, "kind": kind,
                "sample": f"{args.ref_steps} KDK step(s) of the full workload (N={n}) after one warm-up force call"}
 
@@ -807,7 +821,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="disk1m", choices=sorted(WORKLOADS))
-    ap.add_argument("--ref-steps", type=int, default=2, help="KDK steps timed on the CPU")
+    ap.add_argument("--ref-steps", type=int, default=2, help="KDK steps of the CPU baseline leg of the GPU arm")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0,
+                    help="--impl reference: time budget of its timed steps (stops early past it)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--adjoint-steps", type=int, default=1000, help="KDK steps of the adjoint leg")

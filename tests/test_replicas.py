@@ -52,4 +52,5 @@ def test_reference_arm_prints_one_line_from_rank_zero():
     assert len(lines) == 1
     d = lines[0]
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["steps"] == 1 and d["warmup"] == 0  # the arm times the requested steps
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("reference", "port")
