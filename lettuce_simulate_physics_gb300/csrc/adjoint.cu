@@ -17,8 +17,10 @@
 //   dL/dx_k += G sum_j M(d_kj) (m_k w_j - m_j w_k),  M(d) u = u / s^3 - 3 d (d . u) / s^5
 //   dL/dm_k -= G sum_j (w_j . d_kj) / s^3
 // The self pair contributes exactly zero (d = 0, u = 0). Pair arithmetic is FP32 on block-relative
-// coordinates from the FP64 hi/lo split, packed f32x2; sums across tiles are Kahan-compensated and
-// the adjoint state is accumulated in FP64.
+// coordinates from the FP64 hi/lo split, packed f32x2; the adjoint state is accumulated in FP64.
+// Two kernels: k_vjp evaluates every ordered pair (split-j, Kahan across tiles) and serves small
+// systems; k_vjp_sym evaluates every unordered pair once for both bodies (tile-pair units, partial
+// sums added in FP64) and serves systems of about 26k bodies and more.
 //
 // Checkpoints: FP64 positions and FP32 velocities every k steps; the backward pass restores each
 // segment, recomputes its positions with the same deterministic kernels (so they are bit-identical
@@ -204,6 +206,234 @@ __global__ void k_vjp_apply(const float4* __restrict__ partial, int n, int slice
     lm[i] -= G * h;
 }
 
+// ---- symmetric pairwise VJP ------------------------------------------------------------------
+// Each unordered pair (k, j), k < j, is evaluated once. With d = x_j - x_k, s^2 = |d|^2 + eps^2 and
+// cc = (m_k (w_j . d) - m_j (w_k . d)) / s^5, the pair adds to body k (the i side)
+//   S1 += w_j / s^3,  -S2 += -m_j / s^3,  S3 += cc d,  h += (w_j . d) / s^3
+// and to body j (the j side: d_jk = -d and the same cc)
+//   S1 += w_k / s^3,  S2 += m_k / s^3,  S3 -= cc d,  h -= (w_k . d) / s^3,
+// which is 34 FP32 operations for two ordered pairs instead of 52. Work units are pairs of
+// STILE-body tiles (I, J), J >= I; a block takes a strip of up to SSTRIP J tiles for one I tile,
+// its threads holding SIPT i-bodies each. The i side sums in registers over the strip. The j side
+// of each pair of j-bodies is summed over a warp's lanes by a transposed butterfly (16 values over
+// 32 lanes: each exchange sends half of what a lane holds), over the block's warps in shared
+// memory (warp order), and stored per unit. A diagonal unit (J == I) masks the pairs j <= k. All
+// sums run in a fixed order, so results do not depend on scheduling; k_vjp_sym_apply adds the
+// strips' and units' partial sums per body in FP64.
+#ifndef LG_VJPS_BS
+#define LG_VJPS_BS 128
+#endif
+#ifndef LG_VJPS_IPT
+#define LG_VJPS_IPT 4
+#endif
+#ifndef LG_VJPS_MINB
+#define LG_VJPS_MINB 3
+#endif
+constexpr int SBS = LG_VJPS_BS;        // threads per block
+constexpr int SIPT = LG_VJPS_IPT;      // i-bodies per thread
+constexpr int STILE = SBS * SIPT;      // bodies per tile
+constexpr int SSUB = 64;               // j-bodies between cross-warp reductions
+constexpr int SSTRIP = 2;              // J tiles per block
+constexpr int SWARPS = SBS / 32;
+static_assert(STILE % SSUB == 0 && SSUB % 2 == 0, "sub-tiles hold whole j pairs");
+
+struct __align__(16) SymSmem {
+    float jx[STILE], jy[STILE], jz[STILE], jnm[STILE], jwx[STILE], jwy[STILE], jwz[STILE];
+    float red[SWARPS][SSUB][8];
+};
+
+// One exchange of the transposed butterfly: lanes with bit O keep the upper H of their 2H values
+// and send the lower H, the others the reverse; each kept value adds the partner's sent one.
+template <int O, int H>
+__device__ __forceinline__ void tr_level(float (&v)[16], int lane) {
+    const bool up = (lane & O) != 0;
+#pragma unroll
+    for (int t = 0; t < H; ++t) {
+        const float send = up ? v[t] : v[t + H];
+        const float keep = up ? v[t + H] : v[t];
+        v[t] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+    }
+}
+
+constexpr float kFarV = 1e18f;  // a far, massless, zero-weight body: adds nothing to either side
+
+// Row I of the j sums holds bodies [I STILE, npad) (the tiles J >= I), rows back to back.
+__device__ __forceinline__ size_t jrow(int I, int npad) {
+    return static_cast<size_t>(I) * npad - static_cast<size_t>(STILE) * (static_cast<size_t>(I) * (I - 1) / 2);
+}
+
+// units[b] = (I, J0, J1, strip): block b evaluates tile I against tiles [J0, J1) and writes its i
+// sums to row `strip` of ipart (the tile's STILE bodies); the j sums of unit (I, J) go to row I of
+// jpart. Entries are 8 floats: S1 (3), -S2, S3 (3), h, where jpart holds the j side's -S2, S3 and
+// h with the opposite sign.
+template <bool EPS0>
+__global__ void __launch_bounds__(SBS, LG_VJPS_MINB) k_vjp_sym(const float4* __restrict__ hm, const float4* __restrict__ lo,
+                                                   const float4* __restrict__ wv, int n, int npad, float e2,
+                                                   const int4* __restrict__ units, float* __restrict__ ipart,
+                                                   float* __restrict__ jpart) {
+    __shared__ SymSmem sm;
+    const int4 un = units[blockIdx.x];
+    const int I = un.x, J0 = un.y, J1 = un.z, strip = un.w;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ib = I * STILE;
+    const float4 oh = hm[ib], ol = lo[ib];  // the block origin: the tile's first body (ib < n)
+    f2x XI[SIPT], YI[SIPT], ZI[SIPT], MK[SIPT], WKX[SIPT], WKY[SIPT], WKZ[SIPT];
+    f2x a[SIPT][8];
+    int iidx[SIPT];
+#pragma unroll
+    for (int u = 0; u < SIPT; ++u) {
+        const int i = ib + u * SBS + tid;
+        iidx[u] = i;
+        float x = kFarV, y = kFarV, z = kFarV, m = 0.f;
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < n) {  // past n: far, massless, zero weight, so it adds nothing to either side
+            const float4 h = hm[i], l = lo[i];
+            w = wv[i];
+            x = (h.x - oh.x) + (l.x - ol.x);
+            y = (h.y - oh.y) + (l.y - ol.y);
+            z = (h.z - oh.z) + (l.z - ol.z);
+            m = h.w;
+        }
+        XI[u] = f2_bcast(x); YI[u] = f2_bcast(y); ZI[u] = f2_bcast(z);
+        MK[u] = f2_bcast(m);
+        WKX[u] = f2_bcast(w.x); WKY[u] = f2_bcast(w.y); WKZ[u] = f2_bcast(w.z);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[u][q] = 0ull;
+    }
+    const f2x E2 = f2_bcast(e2);
+    // The (j, component) a lane holds after the butterfly: lane bits 4..1 select halves in turn.
+    const int qsel = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+    for (int J = J0; J < J1; ++J) {
+        const int jb = J * STILE;
+        __syncthreads();  // the previous tile's readers are done
+        for (int k = tid; k < STILE; k += SBS) {
+            const int j = jb + k;
+            if (j < n) {
+                const float4 h = hm[j], l = lo[j], w = wv[j];
+                sm.jx[k] = (h.x - oh.x) + (l.x - ol.x);
+                sm.jy[k] = (h.y - oh.y) + (l.y - ol.y);
+                sm.jz[k] = (h.z - oh.z) + (l.z - ol.z);
+                sm.jnm[k] = -h.w;
+                sm.jwx[k] = w.x; sm.jwy[k] = w.y; sm.jwz[k] = w.z;
+            } else {
+                sm.jx[k] = sm.jy[k] = sm.jz[k] = kFarV;
+                sm.jnm[k] = 0.f;
+                sm.jwx[k] = sm.jwy[k] = sm.jwz[k] = 0.f;
+            }
+        }
+        __syncthreads();
+        const bool diag = J == I;
+        for (int s0 = 0; s0 < STILE; s0 += SSUB) {
+            for (int jp = s0; jp < s0 + SSUB; jp += 2) {
+                const f2x X = ld2(sm.jx + jp), Y = ld2(sm.jy + jp), Z = ld2(sm.jz + jp), NM = ld2(sm.jnm + jp);
+                const f2x WX = ld2(sm.jwx + jp), WY = ld2(sm.jwy + jp), WZ = ld2(sm.jwz + jp);
+                f2x b[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) b[q] = 0ull;
+#pragma unroll
+                for (int u = 0; u < SIPT; ++u) {
+                    const f2x dx = f2_sub(X, XI[u]), dy = f2_sub(Y, YI[u]), dz = f2_sub(Z, ZI[u]);
+                    const f2x r2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, E2)));
+                    float ra, rb;
+                    f2_unpack(r2, ra, rb);
+                    float ia = rsqrt_mufu(ra), ibb = rsqrt_mufu(rb);
+                    if (EPS0) {
+                        ia = ra > 0.f ? ia : 0.f;
+                        ibb = rb > 0.f ? ibb : 0.f;
+                    }
+                    if (diag) {  // only pairs j > k: the tile's own lower triangle and self pairs add nothing
+                        const int jg = jb + jp;
+                        ia = jg > iidx[u] ? ia : 0.f;
+                        ibb = jg + 1 > iidx[u] ? ibb : 0.f;
+                    }
+                    const f2x inv = f2_pack(ia, ibb);
+                    const f2x inv2 = f2_mul(inv, inv), inv3 = f2_mul(inv2, inv), inv5 = f2_mul(inv3, inv2);
+                    const f2x dwj = f2_fma(dx, WX, f2_fma(dy, WY, f2_mul(dz, WZ)));
+                    const f2x dwk = f2_fma(dx, WKX[u], f2_fma(dy, WKY[u], f2_mul(dz, WKZ[u])));
+                    const f2x cc = f2_mul(f2_fma(MK[u], dwj, f2_mul(NM, dwk)), inv5);
+                    a[u][0] = f2_fma(WX, inv3, a[u][0]);
+                    a[u][1] = f2_fma(WY, inv3, a[u][1]);
+                    a[u][2] = f2_fma(WZ, inv3, a[u][2]);
+                    a[u][3] = f2_fma(NM, inv3, a[u][3]);
+                    a[u][4] = f2_fma(cc, dx, a[u][4]);
+                    a[u][5] = f2_fma(cc, dy, a[u][5]);
+                    a[u][6] = f2_fma(cc, dz, a[u][6]);
+                    a[u][7] = f2_fma(dwj, inv3, a[u][7]);
+                    b[0] = f2_fma(WKX[u], inv3, b[0]);
+                    b[1] = f2_fma(WKY[u], inv3, b[1]);
+                    b[2] = f2_fma(WKZ[u], inv3, b[2]);
+                    b[3] = f2_fma(MK[u], inv3, b[3]);
+                    b[4] = f2_fma(cc, dx, b[4]);
+                    b[5] = f2_fma(cc, dy, b[5]);
+                    b[6] = f2_fma(cc, dz, b[6]);
+                    b[7] = f2_fma(dwk, inv3, b[7]);
+                }
+                // v[2c + h] = component c of j-body jp + h, summed over the lane's i-bodies.
+                float v[16];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) f2_unpack(b[c], v[2 * c], v[2 * c + 1]);
+                tr_level<16, 8>(v, lane);
+                tr_level<8, 4>(v, lane);
+                tr_level<4, 2>(v, lane);
+                tr_level<2, 1>(v, lane);
+                v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+                if (!(lane & 1)) sm.red[warp][jp - s0 + (qsel & 1)][qsel >> 1] = v[0];
+            }
+            __syncthreads();
+            // The sub-tile's j sums over the block's warps, in warp order.
+            for (int t = tid; t < SSUB * 8; t += SBS) {
+                const int jj = t >> 3, c = t & 7;
+                float sum = sm.red[0][jj][c];
+#pragma unroll
+                for (int w = 1; w < SWARPS; ++w) sum += sm.red[w][jj][c];
+                const int j = jb + s0 + jj;
+                if (j < n) jpart[(jrow(I, npad) + (j - ib)) * 8 + c] = sum;
+            }
+            __syncthreads();  // red is rewritten by the next sub-tile
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < SIPT; ++u) {
+        if (iidx[u] >= n) continue;
+        float* o = ipart + (static_cast<size_t>(strip) * STILE + (iidx[u] - ib)) * 8;
+        const float4 p0 = make_float4(f2_sum(a[u][0]), f2_sum(a[u][1]), f2_sum(a[u][2]), f2_sum(a[u][3]));
+        const float4 p1 = make_float4(f2_sum(a[u][4]), f2_sum(a[u][5]), f2_sum(a[u][6]), f2_sum(a[u][7]));
+        reinterpret_cast<float4*>(o)[0] = p0;
+        reinterpret_cast<float4*>(o)[1] = p1;
+    }
+}
+
+// Per body k of tile K: the i sums of K's strips and the j sums of units (I, K), I <= K, in that
+// order in FP64; then lx += G (m_k S1 - w_k S2 - 3 S3), lm -= G h.
+__global__ void k_vjp_sym_apply(const float* __restrict__ ipart, const float* __restrict__ jpart,
+                                const int* __restrict__ strip_base, const float4* __restrict__ hm,
+                                const float4* __restrict__ wv, int n, int npad, double G, double* lx, double* ly,
+                                double* lz, double* lm) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int K = k / STILE;
+    double S[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int st = strip_base[K]; st < strip_base[K + 1]; ++st) {
+        const float4* p = reinterpret_cast<const float4*>(ipart + (static_cast<size_t>(st) * STILE + (k - K * STILE)) * 8);
+        const float4 p0 = p[0], p1 = p[1];
+        S[0] += p0.x; S[1] += p0.y; S[2] += p0.z; S[3] += p0.w;
+        S[4] += p1.x; S[5] += p1.y; S[6] += p1.z; S[7] += p1.w;
+    }
+    for (int I = 0; I <= K; ++I) {
+        const float4* p = reinterpret_cast<const float4*>(jpart + (jrow(I, npad) + (k - I * STILE)) * 8);
+        const float4 p0 = p[0], p1 = p[1];
+        S[0] += p0.x; S[1] += p0.y; S[2] += p0.z; S[3] -= p0.w;
+        S[4] -= p1.x; S[5] -= p1.y; S[6] -= p1.z; S[7] -= p1.w;
+    }
+    const double m = hm[k].w;
+    const float4 w = wv[k];
+    // m_k S1 - w_k S2 - 3 S3 (S[3] holds -S2)
+    lx[k] += G * (m * S[0] + w.x * S[3] - 3.0 * S[4]);
+    ly[k] += G * (m * S[1] + w.y * S[3] - 3.0 * S[5]);
+    lz[k] += G * (m * S[2] + w.z * S[3] - 3.0 * S[6]);
+    lm[k] -= G * S[7];
+}
+
 // lv += dt lx; w = c lv (FP32 for the VJP), with the body's mass alongside.
 __global__ void k_adj_kick(const double* lx, const double* ly, const double* lz, double* lvx, double* lvy,
                            double* lvz, double dt, double c, float4* w, int n) {
@@ -348,6 +578,9 @@ struct AdjointState {
     DevBuf seg_x, seg_y, seg_z, seg_id;            // tree: one segment's sorted FP64 positions and ids
     DevBuf m_by_id, w_sorted, gbuf;                // tree: masses by id, weights in body order, VJP output
     DevBuf lx, ly, lz, lvx, lvy, lvz, lm, loss_terms, w, partial;
+    DevBuf sym_units, sym_sbase, ipart, jpart;     // direct: the symmetric VJP's schedule and partial sums
+    std::vector<int4> sym_units_h;                 // (host copies, alive while their uploads run)
+    std::vector<int> sym_sbase_h;
     DevBuf tx, ty, tz;
     bool have_forward = false;
 };
@@ -542,7 +775,43 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     int slices = std::max(1, std::min(n / 128 + 1, (vjp_per_sm * e.sms + iblocks - 1) / iblocks));
     int jslice = (n + slices - 1) / slices;
     slices = (n + jslice - 1) / jslice;
-    if (!tree) a.partial.reserve(static_cast<size_t>(slices) * n * 16);
+    // Symmetric VJP (each unordered pair once) when there are enough tile units to fill the GPU
+    // (at least four per SM: about 26k bodies and up; below that the one-sided kernel's split-j
+    // grid fills it better) and its unit partial sums stay within 4 GB (about 350k bodies).
+    // LETTUCE_GB300_VJP=pairs or =symmetric overrides the size rule (not the memory bound).
+    const int T = (n + STILE - 1) / STILE;
+    const int npad = T * STILE;
+    const size_t jbytes = static_cast<size_t>(STILE) * T * (T + 1) / 2 * 32;
+    long long units_needed = 0;  // one block per strip of up to SSTRIP tiles: sum over I of ceil((T - I) / SSTRIP)
+    for (int I = 0; I < T; ++I) units_needed += (T - I + SSTRIP - 1) / SSTRIP;
+    bool sym = !tree && jbytes <= (size_t(4) << 30) && units_needed >= 4LL * e.sms;
+    if (const char* v = std::getenv("LETTUCE_GB300_VJP")) {
+        const std::string m = v;
+        if (m != "pairs" && m != "symmetric") fail(kRuntime, "LETTUCE_GB300_VJP must be pairs or symmetric, not '" + m + "'");
+        sym = !tree && jbytes <= (size_t(4) << 30) && m == "symmetric";
+    }
+    int nunits = 0;
+    if (sym) {
+        a.sym_units_h.clear();
+        a.sym_sbase_h.assign(static_cast<size_t>(T) + 1, 0);
+        int strip = 0;
+        for (int I = 0; I < T; ++I) {
+            a.sym_sbase_h[I] = strip;
+            for (int J0 = I; J0 < T; J0 += SSTRIP) a.sym_units_h.push_back(make_int4(I, J0, std::min(T, J0 + SSTRIP), strip++));
+        }
+        a.sym_sbase_h[T] = strip;
+        nunits = static_cast<int>(a.sym_units_h.size());
+        a.sym_units.reserve(a.sym_units_h.size() * sizeof(int4));
+        a.sym_sbase.reserve(a.sym_sbase_h.size() * sizeof(int));
+        LG_CK(cudaMemcpyAsync(a.sym_units.as<int4>(), a.sym_units_h.data(), a.sym_units_h.size() * sizeof(int4),
+                              cudaMemcpyHostToDevice, s));
+        LG_CK(cudaMemcpyAsync(a.sym_sbase.as<int>(), a.sym_sbase_h.data(), a.sym_sbase_h.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, s));
+        a.ipart.reserve(static_cast<size_t>(strip) * STILE * 32);
+        a.jpart.reserve(jbytes);
+    } else if (!tree) {
+        a.partial.reserve(static_cast<size_t>(slices) * n * 16);
+    }
     const float e2 = static_cast<float>(a.p.eps * a.p.eps);
     const bool eps0 = !(e2 >= 1.17549435e-38f);
     const double h = 0.5 * a.dt;
@@ -619,6 +888,23 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
             } else {
                 const float4* hm = a.seg_hm[seg & 1].as<float4>() + so;
                 const float4* lo = a.seg_lo[seg & 1].as<float4>() + so;
+                if (sym) {
+                    if (eps0)
+                        k_vjp_sym<true><<<nunits, SBS, 0, vs>>>(hm, lo, a.w.as<float4>(), n, npad, e2,
+                                                                a.sym_units.as<int4>(), a.ipart.as<float>(),
+                                                                a.jpart.as<float>());
+                    else
+                        k_vjp_sym<false><<<nunits, SBS, 0, vs>>>(hm, lo, a.w.as<float4>(), n, npad, e2,
+                                                                 a.sym_units.as<int4>(), a.ipart.as<float>(),
+                                                                 a.jpart.as<float>());
+                    LG_LAUNCHED();
+                    k_vjp_sym_apply<<<gb, 256, 0, vs>>>(a.ipart.as<float>(), a.jpart.as<float>(), a.sym_sbase.as<int>(),
+                                                        hm, a.w.as<float4>(), n, npad, a.p.G, a.lx.as<double>(),
+                                                        a.ly.as<double>(), a.lz.as<double>(), a.lm.as<double>());
+                    LG_LAUNCHED();
+                    e.launches += 3;
+                    continue;
+                }
                 dim3 grid(iblocks, slices);
                 if (eps0)
                     k_vjp<true><<<grid, VBS, 0, vs>>>(hm, lo, a.w.as<float4>(), n, jslice, e2, a.partial.as<float4>());

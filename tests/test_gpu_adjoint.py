@@ -37,8 +37,10 @@ def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a) - b) / max(np.linalg.norm(b), 1e-300))
 
 
+@pytest.mark.parametrize("vjp", ["symmetric", "pairs"])
 @pytest.mark.parametrize("n,steps,every", [(256, 40, 8), (700, 64, 16), (512, 33, 32)])
-def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, every):
+def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, every, vjp, monkeypatch):
+    monkeypatch.setenv("LETTUCE_GB300_VJP", vjp)
     b = S.plummer(n, 2, cut=10)
     G, eps, dt = 1.0, 0.05, 1e-3
     x0, v0 = b.pos64(), b.vel64()
@@ -74,6 +76,33 @@ def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, ever
         fd = (O.loss_direct_fp64(x0, v0, p, G, eps, dt, steps, xstar)
               - O.loss_direct_fp64(x0, v0, q, G, eps, dt, steps, xstar)) / (2 * h * m[i])
         assert abs(gm[i] - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(gm).max(), (i, gm[i], fd)
+
+
+@pytest.mark.parametrize("eps", [0.02, 0.0])
+def test_symmetric_vjp_equals_one_sided_vjp(be, eps, monkeypatch):
+    """The symmetric pairwise VJP (each unordered pair once; 512-body tiles, strips of two tiles,
+    here ten tiles with a partial last one) gives the one-sided kernel's gradients to FP32 rounding,
+    and repeats itself bit for bit."""
+    b = S.plummer(5000, 9, cut=10)
+    n = len(b)
+    G, dt, steps, every = 1.0, 1e-3, 5, 2
+    rng = np.random.Generator(np.random.PCG64(9))
+    xstar = b.pos64() + rng.normal(0, 1e-2, (n, 3))
+    out = {}
+    for mode in ("pairs", "symmetric", "symmetric"):
+        monkeypatch.setenv("LETTUCE_GB300_VJP", mode)
+        be.upload(b)
+        be.adjoint_forward(L.ForceParams(G=G, eps=eps, method=L.ForceMethod.direct), dt, steps, every)
+        r = be.adjoint_backward(xstar)
+        if mode in out:
+            assert all(np.array_equal(x, y) for x, y in zip(r[1:], out[mode][1:])), "deterministic"
+        out[mode] = r
+    (lp, gxp, gvp, gmp), (ls, gxs, gvs, gms) = out["pairs"], out["symmetric"]
+    e = (_rel(gxs, gxp), _rel(gvs, gvp), _rel(gms, gmp))
+    print(f"eps={eps}: symmetric vs one-sided gx {e[0]:.3g} gv {e[1]:.3g} gm {e[2]:.3g}")
+    assert ls == lp
+    tol = 2e-6 if eps > 0 else 1e-4  # unsoftened close pairs amplify FP32 rounding differences
+    assert max(e) <= tol
 
 
 def test_adjoint_backward_requires_forward(be):
