@@ -33,6 +33,7 @@
 // the backward pass loads those positions and rebuilds the tree: the sort of already sorted bodies
 // is the identity, so the tree, its moments and its lists are bit-identical to the forward pass's.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -213,7 +214,7 @@ __global__ void k_vjp_apply(const float4* __restrict__ partial, int n, int slice
 // and to body j (the j side: d_jk = -d and the same cc)
 //   S1 += w_k / s^3,  S2 += m_k / s^3,  S3 -= cc d,  h -= (w_k . d) / s^3,
 // which is 34 FP32 operations for two ordered pairs instead of 52. Work units are pairs of
-// STILE-body tiles (I, J), J >= I; a block takes a strip of up to SSTRIP J tiles for one I tile,
+// STILE-body tiles (I, J), J >= I; a block takes a strip of SSTRIP J tiles (or fewer) for one I tile,
 // its threads holding SIPT i-bodies each. The i side sums in registers over the strip. The j side
 // of each pair of j-bodies is summed over a warp's lanes by a transposed butterfly (16 values over
 // 32 lanes: each exchange sends half of what a lane holds), over the block's warps in shared
@@ -232,8 +233,11 @@ __global__ void k_vjp_apply(const float4* __restrict__ partial, int n, int slice
 constexpr int SBS = LG_VJPS_BS;        // threads per block
 constexpr int SIPT = LG_VJPS_IPT;      // i-bodies per thread
 constexpr int STILE = SBS * SIPT;      // bodies per tile
+#ifndef LG_VJPS_STRIP
+#define LG_VJPS_STRIP 1
+#endif
 constexpr int SSUB = 64;               // j-bodies between cross-warp reductions
-constexpr int SSTRIP = 2;              // J tiles per block
+constexpr int SSTRIP = LG_VJPS_STRIP;  // J tiles per block
 constexpr int SWARPS = SBS / 32;
 static_assert(STILE % SSUB == 0 && SSUB % 2 == 0, "sub-tiles hold whole j pairs");
 
@@ -322,7 +326,9 @@ __global__ void __launch_bounds__(SBS, LG_VJPS_MINB) k_vjp_sym(const float4* __r
             }
         }
         __syncthreads();
-        const bool diag = J == I;
+        // The tile's sub-tiles, compiled twice: with the diagonal mask (J == I) and without.
+        auto tile = [&](auto diag_tag) {
+        constexpr bool DIAG = decltype(diag_tag)::value;
         for (int s0 = 0; s0 < STILE; s0 += SSUB) {
             for (int jp = s0; jp < s0 + SSUB; jp += 2) {
                 const f2x X = ld2(sm.jx + jp), Y = ld2(sm.jy + jp), Z = ld2(sm.jz + jp), NM = ld2(sm.jnm + jp);
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(SBS, LG_VJPS_MINB) k_vjp_sym(const float4* __r
                         ia = ra > 0.f ? ia : 0.f;
                         ibb = rb > 0.f ? ibb : 0.f;
                     }
-                    if (diag) {  // only pairs j > k: the tile's own lower triangle and self pairs add nothing
+                    if constexpr (DIAG) {  // only pairs j > k: the tile's lower triangle and self pairs add nothing
                         const int jg = jb + jp;
                         ia = jg > iidx[u] ? ia : 0.f;
                         ibb = jg + 1 > iidx[u] ? ibb : 0.f;
@@ -391,6 +397,9 @@ __global__ void __launch_bounds__(SBS, LG_VJPS_MINB) k_vjp_sym(const float4* __r
             }
             __syncthreads();  // red is rewritten by the next sub-tile
         }
+        };
+        if (J == I) tile(std::true_type{});
+        else tile(std::false_type{});
     }
 #pragma unroll
     for (int u = 0; u < SIPT; ++u) {
@@ -777,18 +786,19 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
     slices = (n + jslice - 1) / jslice;
     // Symmetric VJP (each unordered pair once) when there are enough tile units to fill the GPU
     // (at least four per SM: about 26k bodies and up; below that the one-sided kernel's split-j
-    // grid fills it better) and its unit partial sums stay within 4 GB (about 350k bodies).
+    // grid fills it better) and its partial sums stay within 4 GB (about 250k bodies).
     // LETTUCE_GB300_VJP=pairs or =symmetric overrides the size rule (not the memory bound).
     const int T = (n + STILE - 1) / STILE;
     const int npad = T * STILE;
     const size_t jbytes = static_cast<size_t>(STILE) * T * (T + 1) / 2 * 32;
     long long units_needed = 0;  // one block per strip of up to SSTRIP tiles: sum over I of ceil((T - I) / SSTRIP)
     for (int I = 0; I < T; ++I) units_needed += (T - I + SSTRIP - 1) / SSTRIP;
-    bool sym = !tree && jbytes <= (size_t(4) << 30) && units_needed >= 4LL * e.sms;
+    const bool fits = jbytes + static_cast<size_t>(units_needed) * STILE * 32 <= (size_t(4) << 30);
+    bool sym = !tree && fits && units_needed >= 4LL * e.sms;
     if (const char* v = std::getenv("LETTUCE_GB300_VJP")) {
         const std::string m = v;
         if (m != "pairs" && m != "symmetric") fail(kRuntime, "LETTUCE_GB300_VJP must be pairs or symmetric, not '" + m + "'");
-        sym = !tree && jbytes <= (size_t(4) << 30) && m == "symmetric";
+        sym = !tree && fits && m == "symmetric";
     }
     int nunits = 0;
     if (sym) {

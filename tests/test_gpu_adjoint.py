@@ -80,7 +80,7 @@ def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, ever
 
 @pytest.mark.parametrize("eps", [0.02, 0.0])
 def test_symmetric_vjp_equals_one_sided_vjp(be, eps, monkeypatch):
-    """The symmetric pairwise VJP (each unordered pair once; 512-body tiles, strips of two tiles,
+    """The symmetric pairwise VJP (each unordered pair once; 512-body tiles, one block per tile pair,
     here ten tiles with a partial last one) gives the one-sided kernel's gradients to FP32 rounding,
     and repeats itself bit for bit."""
     b = S.plummer(5000, 9, cut=10)
