@@ -232,6 +232,35 @@ def test_forest_key_restarts_bit_exact():
         assert np.array_equal(ga.view(np.uint32), ra.view(np.uint32)), k
 
 
+def test_forest_nested_key_restarts_bit_exact():
+    """A tree system whose bodies sit at radii log-uniform over 30 decades needs key restarts
+    within key restarts (a 101-level tree) in the forest as in a plain engine: forces agree bit
+    for bit, and the other systems are untouched by its frames."""
+    from gpu_util import deep_radial
+    b, counts, eps, theta, methods = S.ensemble(sizes=[3000, 20000, 12000], direct_max=DIRECT_MAX, theta=0.5)
+    lo, n1 = int(counts[0]), int(counts[1])
+    d = deep_radial(n1, 5, 30)
+    b.x[lo:lo + n1], b.y[lo:lo + n1], b.z[lo:lo + n1] = d.x, d.y, d.z
+    wl = (b, counts, eps, theta, methods)
+    en = ensemble_from(wl)
+    en.energy()
+    a = en.accel()
+    got = en.download()
+    off = offsets(counts)
+    tun = en.tuning()
+    for k in range(len(counts)):
+        s0, s1 = int(off[k]), int(off[k + 1])
+        ga = by_local_id(got.id[s0:s1] - s0, a[:, s0:s1])
+        be = plain_engine(k, wl, tun)
+        be.upload(system_bodies(b, s0, s1))
+        be.compute_forces(plain_params(k, wl), True)
+        if k == 1:
+            assert be.tree_counts()["max_depth"] > 4 * 21
+        ra = by_local_id(be.download().id, be.accel())
+        be.close()
+        assert np.array_equal(ga.view(np.uint32), ra.view(np.uint32)), k
+
+
 def test_energy_per_system(workload):
     b, counts, eps, theta, methods = workload
     en = ensemble_from(workload)
