@@ -234,9 +234,12 @@ constexpr int SBS = LG_VJPS_BS;        // threads per block
 constexpr int SIPT = LG_VJPS_IPT;      // i-bodies per thread
 constexpr int STILE = SBS * SIPT;      // bodies per tile
 #ifndef LG_VJPS_STRIP
-#define LG_VJPS_STRIP 1
+#define LG_VJPS_STRIP 2
 #endif
-constexpr int SSUB = 64;               // j-bodies between cross-warp reductions
+#ifndef LG_VJPS_SUB
+#define LG_VJPS_SUB 128
+#endif
+constexpr int SSUB = LG_VJPS_SUB;      // j-bodies between cross-warp reductions
 constexpr int SSTRIP = LG_VJPS_STRIP;  // J tiles per block
 constexpr int SWARPS = SBS / 32;
 static_assert(STILE % SSUB == 0 && SSUB % 2 == 0, "sub-tiles hold whole j pairs");
@@ -810,6 +813,9 @@ double adjoint_backward(Engine& e, AdjointState& a, const double* tx, const doub
             for (int J0 = I; J0 < T; J0 += SSTRIP) a.sym_units_h.push_back(make_int4(I, J0, std::min(T, J0 + SSTRIP), strip++));
         }
         a.sym_sbase_h[T] = strip;
+        // Whole strips first, the shorter ones last: the grid's last wave holds the smallest blocks.
+        std::stable_sort(a.sym_units_h.begin(), a.sym_units_h.end(),
+                         [](const int4& p, const int4& q) { return p.z - p.y > q.z - q.y; });
         nunits = static_cast<int>(a.sym_units_h.size());
         a.sym_units.reserve(a.sym_units_h.size() * sizeof(int4));
         a.sym_sbase.reserve(a.sym_sbase_h.size() * sizeof(int));
