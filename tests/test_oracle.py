@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from golden_io import Golden, by_id, names, rel_rms
+from gpu_util import deep_radial
 from lettuce_simulate_physics_gb300 import scenarios as S
 from oracle import oracle as O
 
@@ -127,6 +128,28 @@ def test_port_vs_live_reference(n, seed, kind):
     assert np.array_equal(p.groups(), r.groups())
     assert p.times()["interactions"] == r.times()["interactions"]
     assert rel_rms(p.accel()[:3], r.accel()[:3]) <= 1e-6
+
+
+@pytest.mark.skipif(not O.available("ref"), reason="reference sources not present: golden vectors pin the port")
+@pytest.mark.parametrize("n,decades", [(20000, 30), (30000, 37)])
+def test_port_nested_rekeys_vs_live_reference(n, decades):
+    """Radii log-uniform over 30 and 37 decades: the reference re-keys runs inside re-keyed runs
+    (src/cpu_backend.cpp:536-544) down to depth 101 and 124; the port's recursion gives the same
+    keys (each body's last frame), permutation, nodes, cell geometry, groups and lists."""
+    b = deep_radial(n, 5, decades)
+    p = _run("port", b, O.TREE, 1.0, 0.01, 0.5, False)
+    r = _run("ref", b, O.TREE, 1.0, 0.01, 0.5, False)
+    assert p.max_depth() == r.max_depth() > 4 * 21
+    assert np.array_equal(p.keys(), r.keys())
+    assert np.array_equal(p.download().id, r.download().id)
+    pn, rn = p.nodes(), r.nodes()
+    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qzz"):
+        assert np.array_equal(pn[f], rn[f]), f
+    pg, rg = p.geo(), r.geo()
+    for f in ("gx", "gy", "gz", "half"):
+        assert np.array_equal(pg[f], rg[f]), f
+    assert np.array_equal(p.groups(), r.groups())
+    assert p.times()["interactions"] == r.times()["interactions"]
 
 
 def test_fp64_adjoint_matches_central_differences():
