@@ -126,6 +126,15 @@ def main():
     b = b.append(Bodies.from_arrays(np.array([[1e8, 0, 0]]), np.zeros((1, 3)), np.array([b.m[0]], np.float64)))
     save("tree_escaper_dup3001", b, dict(G=G, eps=0.05), t00=force_case(b, O.TREE, G, 0.05, 0.0, True),
          t06=force_case(b, O.TREE, G, 0.05, 0.6, True))
+    # Radii log-uniform over 34 decades (down to 1e-34): runs of identical keys are re-keyed again
+    # and again (src/cpu_backend.cpp:536-544), a 113-level tree with five key frames.
+    rng = np.random.Generator(np.random.PCG64(6))
+    n = 10000
+    u = rng.normal(size=(n, 3))
+    p = u / np.linalg.norm(u, axis=1)[:, None] * (10.0 ** rng.uniform(-34, 0, n))[:, None]
+    b = Bodies.from_arrays(p, np.zeros((n, 3)), np.full(n, 1.0 / n))
+    save("tree_deep10000", b, dict(G=G, eps=0.01), t06=force_case(b, O.TREE, G, 0.01, 0.6, True),
+         t00=force_case(b, O.TREE, G, 0.01, 0.0, False))
     # Small and odd N, direct and tree(theta=0) (:200-221 shape).
     for n in (1, 2, 3, 31, 32, 33, 64, 255, 257, 1000, 1023):
         b = S.cube(n, 100 + n)
