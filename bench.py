@@ -327,7 +327,7 @@ def ensemble_leg(L, local, steps=200, seq_steps=10, count=512):
     return {
         "systems": int(len(counts)), "n_total": n, "n_tree_systems": int((methods == 1).sum()),
         "n_direct_systems": int((methods == 0).sum()), "steps": steps, "dt": dt,
-        "tuning": {"direct_ipt": list(tun.direct_ipt), "walk_group": tun.walk_group, "tune_s": round(tune_s, 2)},
+        "tuning": {"direct_ipt": list(tun.direct_ipt), "direct_tile": list(tun.direct_tile), "walk_group": tun.walk_group, "tune_s": round(tune_s, 2)},
         "batched": {"run_ms": round(st.run_ms, 3), "wall_s": round(wall, 4), "used_graph": st.used_graph,
                     "recoveries": st.recoveries, "launches_per_step": st.launches_per_step,
                     "bodies_steps_per_s": batched_dev, "bodies_steps_per_s_wall": batched_wall,

@@ -283,12 +283,14 @@ typedef struct {
     unsigned long long last_interactions; /* body pairs + cell terms of the last force phase */
 } lg_ensemble_stats;
 
-/* Tuning: i-bodies per thread of the batched direct kernel for systems with N < 2048, N < 4096
- * and larger (classes 0-2), and the walk group size of the forest tree. */
+/* Tuning: i-bodies per thread (1, 2, 4 or 8) and j-bodies per shared-memory stage (256, or 128
+ * with 1, 2 or 4 i-bodies per thread) of the batched direct kernel for systems with N < 2048,
+ * N < 4096 and larger (classes 0-2), and the walk group size of the forest tree. */
 typedef struct {
     int direct_ipt[3];
     int walk_group;
     int tuned;              /* 1 after lg_ensemble_tune measured or loaded them */
+    int direct_tile[3];
 } lg_ensemble_tuning;
 
 lg_status lg_ensemble_create(int device, lg_ensemble** out);

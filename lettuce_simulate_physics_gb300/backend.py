@@ -117,7 +117,7 @@ class _CEnsStats(C.Structure):
 
 
 class _CEnsTuning(C.Structure):
-    _fields_ = [("direct_ipt", C.c_int * 3), ("walk_group", C.c_int), ("tuned", C.c_int)]
+    _fields_ = [("direct_ipt", C.c_int * 3), ("walk_group", C.c_int), ("tuned", C.c_int), ("direct_tile", C.c_int * 3)]
 
 
 # LetNode (src/backend.hpp:62-75): the 60-byte record of a locally-essential tree node.

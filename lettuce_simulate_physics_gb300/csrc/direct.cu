@@ -1,7 +1,7 @@
 // Direct summation (the reference's direct<POT>, src/cpu_backend.cpp:353-392, and direct_kernel,
 // src/cuda_backend.cu:301-350), GB300 form:
 //  - each thread keeps IPT i-bodies in registers;
-//  - j-bodies stream through shared memory in tiles of TILE float4 (hi x, hi y, hi z, m) plus the
+//  - j-bodies stream through shared memory in tiles of TL (256, or 128) float4 (hi x, hi y, hi z, m) plus the
 //    float4 low parts, fetched by the TMA engine (cp.async.bulk, mbarrier completion) into two
 //    stages, so the copy of tile t+2 overlaps the arithmetic on tile t;
 //  - each tile is converted once per block to coordinates relative to the block origin o (the
@@ -36,25 +36,26 @@ namespace {
 #endif
 constexpr int DUNROLL = LG_DIRECT_UNROLL;
 constexpr int DBS = 256;   // threads per block
-constexpr int TILE = 256;  // j-bodies per stage
+constexpr int TILE = 256;  // j-bodies per stage (default; 128 is the other compiled shape)
 
+template <int TL>
 struct alignas(16) DirectSmem {
-    float4 raw_hm[2][TILE];
-    float4 raw_lo[2][TILE];
-    float rx[2][TILE], ry[2][TILE], rz[2][TILE], rm[2][TILE];
+    float4 raw_hm[2][TL];
+    float4 raw_lo[2][TL];
+    float rx[2][TL], ry[2][TL], rz[2][TL], rm[2][TL];
     uint64_t bar[2];
 };
 
 // One block's work: i-bodies [base, base + DBS * IPT) clipped to iend, against j-bodies [j0, j1).
 // write_final: out[i] = G-scaled sums; otherwise out[i] = unscaled partial sums (out points at the
 // slice's row).
-template <int IPT, bool POT, bool EPS0>
-__device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __restrict__ hm,
+template <int IPT, int TL, bool POT, bool EPS0>
+__device__ __forceinline__ void direct_block(DirectSmem<TL>& sm, const float4* __restrict__ hm,
                                              const float4* __restrict__ lo, int base, int iend, int j0, int j1,
                                              float G, float e2, float4* __restrict__ out, bool write_final,
                                              unsigned* err, float* __restrict__ cost = nullptr) {
     const int tid = threadIdx.x;
-    const int ntiles = (j1 - j0 + TILE - 1) / TILE;
+    const int ntiles = (j1 - j0 + TL - 1) / TL;
     const int n = iend;
 
     // Block origin: the first i-body of the block.
@@ -90,8 +91,8 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
     }
     __syncthreads();
     auto issue = [&](int t) {
-        const int jt = j0 + t * TILE;
-        const unsigned cnt = static_cast<unsigned>(min(TILE, j1 - jt));
+        const int jt = j0 + t * TL;
+        const unsigned cnt = static_cast<unsigned>(min(TL, j1 - jt));
         const int buf = t & 1;
         mbar_arrive_expect_tx(&sm.bar[buf], 2u * cnt * 16u);
         bulk_g2s(sm.raw_hm[buf], hm + jt, cnt * 16u, &sm.bar[buf]);
@@ -108,7 +109,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
         const int buf = t & 1;
         const unsigned parity = (t >> 1) & 1;
         const bool ok = mbar_wait_bounded(&sm.bar[buf], parity);
-        const int cnt = min(TILE, j1 - (j0 + t * TILE));
+        const int cnt = min(TL, j1 - (j0 + t * TL));
         const int cnt8 = (cnt + 7) & ~7;
         if (ok) {
             for (int k = tid; k < cnt8; k += DBS) {
@@ -145,7 +146,7 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
         // Pairs k, k + 1 of the tile. With the potential, the tiles that hold the block's own
         // bodies take the self pair out by index (its mass half set to zero), as the reference's
         // direct kernel does: no m/eps is added and subtracted, so phi keeps its low bits.
-        const int jt0 = j0 + t * TILE;
+        const int jt0 = j0 + t * TL;
         auto tile_pairs = [&](auto masked) {
             constexpr bool MASK = decltype(masked)::value;
 #pragma unroll DUNROLL
@@ -209,26 +210,26 @@ __device__ __forceinline__ void direct_block(DirectSmem& sm, const float4* __res
     }
 }
 
-template <int IPT, bool POT, bool EPS0>
+template <int IPT, int TL, bool POT, bool EPS0>
 __global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct(const float4* __restrict__ hm, const float4* __restrict__ lo, int n,
                                                 int jslice, float G, float e2, float4* __restrict__ out, int write_final,
                                                 unsigned* err, float* cost) {
-    __shared__ DirectSmem sm;
+    __shared__ DirectSmem<TL> sm;
     const int j0 = blockIdx.y * jslice;
-    direct_block<IPT, POT, EPS0>(sm, hm, lo, blockIdx.x * (DBS * IPT), n, j0, min(n, j0 + jslice), G, e2,
+    direct_block<IPT, TL, POT, EPS0>(sm, hm, lo, blockIdx.x * (DBS * IPT), n, j0, min(n, j0 + jslice), G, e2,
                                  write_final ? out : out + static_cast<size_t>(blockIdx.y) * n, write_final != 0, err,
                                  cost);
 }
 
 // Many independent systems in one launch: block b takes work item b (an i-tile of one system
 // against all of that system's bodies), with the system's own softening.
-template <int IPT, bool POT, bool EPS0>
+template <int IPT, int TL, bool POT, bool EPS0>
 __global__ void __launch_bounds__(DBS, LG_DIRECT_MINB) k_direct_batch(const float4* __restrict__ hm, const float4* __restrict__ lo,
                                                       const DirectWork* __restrict__ work, float G,
                                                       float4* __restrict__ acc, unsigned* err) {
-    __shared__ DirectSmem sm;
+    __shared__ DirectSmem<TL> sm;
     const DirectWork w = work[blockIdx.x];
-    direct_block<IPT, POT, EPS0>(sm, hm, lo, w.base, w.iend, w.j0, w.j1, G, w.e2, acc, true, err);
+    direct_block<IPT, TL, POT, EPS0>(sm, hm, lo, w.base, w.iend, w.j0, w.j1, G, w.e2, acc, true, err);
 }
 
 // Sums the split-j partials in slice order (Kahan) and scales by G.
@@ -248,16 +249,16 @@ __global__ void k_direct_reduce(const float4* __restrict__ partial, int n, int s
     acc[i] = make_float4(G * (s[0] - c[0]), G * (s[1] - c[1]), G * (s[2] - c[2]), -G * (s[3] - c[3]));
 }
 
-template <int IPT>
+template <int IPT, int TL>
 void launch_ipt(const BodyArrays b, int n, float G, float e2, bool pot, bool eps0, int jslice, int slices, float4* out,
                 int write_final, unsigned* err, float* cost, cudaStream_t s) {
     dim3 grid((n + DBS * IPT - 1) / (DBS * IPT), slices);
     if (pot) {
-        if (eps0) k_direct<IPT, true, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
-        else k_direct<IPT, true, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        if (eps0) k_direct<IPT, TL, true, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        else k_direct<IPT, TL, true, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
     } else {
-        if (eps0) k_direct<IPT, false, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
-        else k_direct<IPT, false, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        if (eps0) k_direct<IPT, TL, false, true><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
+        else k_direct<IPT, TL, false, false><<<grid, DBS, 0, s>>>(b.hm, b.lo, n, jslice, G, e2, out, write_final, err, cost);
     }
     LG_LAUNCHED();
 }
@@ -271,10 +272,10 @@ int blocks_per_sm(int ipt) {
         int per = 0;
         cudaError_t e = cudaSuccess;
         switch (k) {
-            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<1, false, false>, DBS, 0); break;
-            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<2, false, false>, DBS, 0); break;
-            case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<8, false, false>, DBS, 0); break;
-            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<4, false, false>, DBS, 0); break;
+            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<1, TILE, false, false>, DBS, 0); break;
+            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<2, TILE, false, false>, DBS, 0); break;
+            case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<8, TILE, false, false>, DBS, 0); break;
+            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_direct<4, TILE, false, false>, DBS, 0); break;
         }
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -322,11 +323,20 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
     slices = (n + jslice - 1) / jslice;
     const bool final_out = slices == 1;
     float4* out = final_out ? acc : partial;
-    switch (shape.ipt) {
-        case 1: launch_ipt<1>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
-        case 2: launch_ipt<2>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
-        case 8: launch_ipt<8>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
-        default: launch_ipt<4>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, final_out ? cost : nullptr, s); break;
+    float* c = final_out ? cost : nullptr;
+    if (shape.tile == 128) {  // the other compiled tile shape (1, 2 or 4 i-bodies per thread)
+        switch (shape.ipt) {
+            case 1: launch_ipt<1, 128>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+            case 2: launch_ipt<2, 128>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+            default: launch_ipt<4, 128>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+        }
+    } else {
+        switch (shape.ipt) {
+            case 1: launch_ipt<1, TILE>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+            case 2: launch_ipt<2, TILE>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+            case 8: launch_ipt<8, TILE>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+            default: launch_ipt<4, TILE>(b, n, G, e2, potential, eps0, jslice, slices, out, final_out, err, c, s); break;
+        }
     }
     if (!final_out) {
         k_direct_reduce<<<(n + 255) / 256, 256, 0, s>>>(partial, n, slices, G, acc, cost);
@@ -335,15 +345,15 @@ void launch_direct(const BodyArrays b, int n, float G, float e2, bool potential,
 }
 
 namespace {
-template <int IPT>
+template <int IPT, int TL>
 void launch_batch_ipt(const BodyArrays b, const DirectWork* work, int nwork, float G, bool pot, bool eps0, float4* acc,
                       unsigned* err, cudaStream_t s) {
     if (pot) {
-        if (eps0) k_direct_batch<IPT, true, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
-        else k_direct_batch<IPT, true, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        if (eps0) k_direct_batch<IPT, TL, true, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        else k_direct_batch<IPT, TL, true, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
     } else {
-        if (eps0) k_direct_batch<IPT, false, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
-        else k_direct_batch<IPT, false, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        if (eps0) k_direct_batch<IPT, TL, false, true><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
+        else k_direct_batch<IPT, TL, false, false><<<nwork, DBS, 0, s>>>(b.hm, b.lo, work, G, acc, err);
     }
     LG_LAUNCHED();
 }
@@ -351,14 +361,22 @@ void launch_batch_ipt(const BodyArrays b, const DirectWork* work, int nwork, flo
 
 int direct_block_bodies(int ipt) { return DBS * ipt; }
 
-void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, float G, bool potential,
-                         bool eps0, float4* acc, unsigned* err, cudaStream_t s) {
+void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, int tile, float G,
+                         bool potential, bool eps0, float4* acc, unsigned* err, cudaStream_t s) {
     if (nwork <= 0) return;
-    switch (ipt) {
-        case 1: launch_batch_ipt<1>(b, work, nwork, G, potential, eps0, acc, err, s); break;
-        case 2: launch_batch_ipt<2>(b, work, nwork, G, potential, eps0, acc, err, s); break;
-        case 8: launch_batch_ipt<8>(b, work, nwork, G, potential, eps0, acc, err, s); break;
-        default: launch_batch_ipt<4>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+    if (tile == 128) {
+        switch (ipt) {
+            case 1: launch_batch_ipt<1, 128>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+            case 2: launch_batch_ipt<2, 128>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+            default: launch_batch_ipt<4, 128>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+        }
+    } else {
+        switch (ipt) {
+            case 1: launch_batch_ipt<1, TILE>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+            case 2: launch_batch_ipt<2, TILE>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+            case 8: launch_batch_ipt<8, TILE>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+            default: launch_batch_ipt<4, TILE>(b, work, nwork, G, potential, eps0, acc, err, s); break;
+        }
     }
 }
 

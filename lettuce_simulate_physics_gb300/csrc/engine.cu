@@ -63,12 +63,15 @@ Engine::Engine(int device) : dev(device) {
         if (v < 1 || v > 1024) fail(kRuntime, "LETTUCE_GB300_WALK_MERGE_CAP must be in [1, 1024]");
         merge_cap = v;
     }
-    // Direct launch shape override "ipt,slices" (tuning; otherwise chosen per size).
+    // Direct launch shape override "ipt,slices[,tile]" (tuning; otherwise chosen per size).
     if (const char* d = std::getenv("LETTUCE_GB300_DIRECT")) {
-        int ipt = 0, slices = 0;
-        if (std::sscanf(d, "%d,%d", &ipt, &slices) != 2 || (ipt != 1 && ipt != 2 && ipt != 4 && ipt != 8) || slices < 1)
-            fail(kRuntime, std::string("LETTUCE_GB300_DIRECT must be 'ipt,slices' with ipt in {1,2,4,8}, not '") + d + "'");
-        direct_shape_override = DirectShape{ipt, 256, slices};
+        int ipt = 0, slices = 0, tile = 256;
+        const int got = std::sscanf(d, "%d,%d,%d", &ipt, &slices, &tile);
+        if (got < 2 || (ipt != 1 && ipt != 2 && ipt != 4 && ipt != 8) || slices < 1 || (tile != 256 && tile != 128) ||
+            (tile == 128 && ipt == 8))
+            fail(kRuntime, std::string("LETTUCE_GB300_DIRECT must be 'ipt,slices[,tile]' with ipt in {1,2,4,8} and "
+                                       "tile 256, or 128 with ipt in {1,2,4}, not '") + d + "'");
+        direct_shape_override = DirectShape{ipt, tile, slices};
     }
     name += walk_body ? ", per-body walk" : ", group walk " + std::to_string(group_max);
     if (!walk_body) name += walk_merge ? " (packed)" : " (reference groups)";

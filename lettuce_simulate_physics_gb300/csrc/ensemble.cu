@@ -9,7 +9,8 @@
 // engine's body arrays, so one kick-drift pass and one kick pass cover every system.
 //
 // Force phase. The direct systems are cut into work items (an i-tile of one system against all of
-// its bodies) and run as one batched launch per i-bodies-per-thread class, on a second stream
+// its bodies) and run as one batched launch per kernel shape (i-bodies per thread and j-tile, both
+// chosen per size class by the autotuner), on a second stream
 // that overlaps the forest's sort, build and walk; the tree walk takes each group's root and
 // softening from its system. No host read is needed: the tree build takes its sizes from the
 // previous build (with headroom) and a device-side check records a miss in a sticky word.
@@ -43,10 +44,14 @@ constexpr int kClasses = 3;  // direct size classes: N < 2048, N < 4096, larger
 int size_class(uint32_t n) { return n < 2048 ? 0 : (n < 4096 ? 1 : 2); }
 int default_ipt(int cls) { return cls == 0 ? 1 : (cls == 1 ? 2 : 4); }
 constexpr int kIptCandidates[] = {1, 2, 4};
+constexpr int kTileCandidates[] = {256, 128};
 constexpr int kGroupCandidates[] = {64, 96, 128};
+bool valid_shape(int ipt, int tile) {
+    return (ipt == 1 || ipt == 2 || ipt == 4 || ipt == 8) && (tile == 256 || (tile == 128 && ipt != 8));
+}
 
 struct Segment {
-    int first, count, ipt;
+    int first, count, ipt, tile;
 };
 
 }  // namespace
@@ -62,7 +67,10 @@ public:
         cudaDeviceProp prop{};
         LG_CK(cudaGetDeviceProperties(&prop, device));
         device_name_ = prop.name;
-        for (int c = 0; c < kClasses; ++c) tuning_.direct_ipt[c] = default_ipt(c);
+        for (int c = 0; c < kClasses; ++c) {
+            tuning_.direct_ipt[c] = default_ipt(c);
+            tuning_.direct_tile[c] = 256;
+        }
         tuning_.walk_group = e_->group_max;
         tuning_.tuned = 0;
         sticky_.reserve(256);
@@ -295,11 +303,12 @@ public:
             return;
         }
         cudaStream_t s = e.stream;
-        // Direct classes: time each candidate's batched launch over that class's systems alone.
+        // Direct classes: time each candidate shape's batched launch (i-bodies per thread, j-tile)
+        // over that class's systems alone.
         for (int c = 0; c < kClasses; ++c) {
             std::vector<DirectWork> items;
             float best_ms = FLT_MAX;
-            int best = tuning_.direct_ipt[c];
+            int best = tuning_.direct_ipt[c], best_tile = tuning_.direct_tile[c];
             for (int ipt : kIptCandidates) {
                 items.clear();
                 for (int k = nsys_tree_; k < nsys_; ++k)
@@ -310,22 +319,26 @@ public:
                                  cudaMemcpyHostToDevice));
                 const BodyArrays b = e.bodies(e.cur);
                 const int nw = static_cast<int>(items.size());
-                launch_direct_batch(b, tune_work_.as<DirectWork>(), nw, ipt, static_cast<float>(G_), false, false,
-                                    e.acc.as<float4>(), e.err_word(), s);
-                LG_CK(cudaEventRecord(t0_, s));
-                for (int r = 0; r < 5; ++r)
-                    launch_direct_batch(b, tune_work_.as<DirectWork>(), nw, ipt, static_cast<float>(G_), false, false,
-                                        e.acc.as<float4>(), e.err_word(), s);
-                LG_CK(cudaEventRecord(t1_, s));
-                LG_CK(cudaStreamSynchronize(s));
-                float ms = 0;
-                LG_CK(cudaEventElapsedTime(&ms, t0_, t1_));
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = ipt;
+                for (int tile : kTileCandidates) {
+                    launch_direct_batch(b, tune_work_.as<DirectWork>(), nw, ipt, tile, static_cast<float>(G_), false,
+                                        false, e.acc.as<float4>(), e.err_word(), s);
+                    LG_CK(cudaEventRecord(t0_, s));
+                    for (int r = 0; r < 5; ++r)
+                        launch_direct_batch(b, tune_work_.as<DirectWork>(), nw, ipt, tile, static_cast<float>(G_),
+                                            false, false, e.acc.as<float4>(), e.err_word(), s);
+                    LG_CK(cudaEventRecord(t1_, s));
+                    LG_CK(cudaStreamSynchronize(s));
+                    float ms = 0;
+                    LG_CK(cudaEventElapsedTime(&ms, t0_, t1_));
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = ipt;
+                        best_tile = tile;
+                    }
                 }
             }
             tuning_.direct_ipt[c] = best;
+            tuning_.direct_tile[c] = best_tile;
         }
         build_work();
         // Forest walk group size: time the whole tree force phase (sort, build, walk).
@@ -357,8 +370,9 @@ public:
 
     void set_tuning(const lg_ensemble_tuning& t) {
         for (int c = 0; c < kClasses; ++c)
-            if (t.direct_ipt[c] != 1 && t.direct_ipt[c] != 2 && t.direct_ipt[c] != 4 && t.direct_ipt[c] != 8)
-                fail(kArg, "ensemble tuning: direct_ipt must be 1, 2, 4 or 8");
+            if (!valid_shape(t.direct_ipt[c], t.direct_tile[c]))
+                fail(kArg, "ensemble tuning: direct_ipt must be 1, 2, 4 or 8 and direct_tile 256, or 128 with "
+                           "direct_ipt 1, 2 or 4");
         if (t.walk_group < 1 || t.walk_group > 1024) fail(kArg, "ensemble tuning: walk_group must be in [1, 1024]");
         tuning_ = t;
         LG_CK(cudaSetDevice(e_->dev));
@@ -396,8 +410,8 @@ private:
             // Reads the direct systems' positions from the current body set; the forest's sort
             // copies those bodies unchanged into the other set, and writes acc only below n_tree.
             for (const Segment& g : segs_) {
-                launch_direct_batch(b, d_work_.as<DirectWork>() + g.first, g.count, g.ipt, static_cast<float>(G_), pot,
-                                    false, e.acc.as<float4>(), e.err_word(), ds);
+                launch_direct_batch(b, d_work_.as<DirectWork>() + g.first, g.count, g.ipt, g.tile,
+                                    static_cast<float>(G_), pot, false, e.acc.as<float4>(), e.err_word(), ds);
                 ++e.launches;
             }
             if (split) LG_CK(cudaEventRecord(join_, side_));
@@ -525,17 +539,20 @@ private:
     void build_work() {
         segs_.clear();
         std::vector<DirectWork> all;
-        for (int ipt : {1, 2, 4, 8}) {
-            std::vector<DirectWork> items;
-            for (int k = nsys_tree_; k < nsys_; ++k)
-                if (count_[k] > 0 && tuning_.direct_ipt[size_class(count_[k])] == ipt) add_items(items, k, ipt);
-            if (items.empty()) continue;
-            // Longest j-loops first, so the launch's tail is made of short items.
-            std::stable_sort(items.begin(), items.end(),
-                             [](const DirectWork& a, const DirectWork& b) { return a.j1 - a.j0 > b.j1 - b.j0; });
-            segs_.push_back(Segment{static_cast<int>(all.size()), static_cast<int>(items.size()), ipt});
-            all.insert(all.end(), items.begin(), items.end());
-        }
+        for (int ipt : {1, 2, 4, 8})
+            for (int tile : {256, 128}) {
+                std::vector<DirectWork> items;
+                for (int k = nsys_tree_; k < nsys_; ++k) {
+                    const int c = count_[k] > 0 ? size_class(count_[k]) : -1;
+                    if (c >= 0 && tuning_.direct_ipt[c] == ipt && tuning_.direct_tile[c] == tile) add_items(items, k, ipt);
+                }
+                if (items.empty()) continue;
+                // Longest j-loops first, so the launch's tail is made of short items.
+                std::stable_sort(items.begin(), items.end(),
+                                 [](const DirectWork& a, const DirectWork& b) { return a.j1 - a.j0 > b.j1 - b.j0; });
+                segs_.push_back(Segment{static_cast<int>(all.size()), static_cast<int>(items.size()), ipt, tile});
+                all.insert(all.end(), items.begin(), items.end());
+            }
         if (!all.empty()) {
             d_work_.reserve(all.size() * sizeof(DirectWork));
             LG_CK(cudaMemcpy(d_work_.as<DirectWork>(), all.data(), all.size() * sizeof(DirectWork),
@@ -576,6 +593,14 @@ private:
                         found |= 1 << c;
                     }
                 }
+                const std::string kt = cache_key("direct_tile", c);
+                if (line.compare(0, kt.size(), kt) == 0) {
+                    const int v = std::atoi(line.c_str() + kt.size());
+                    if (v == 256 || v == 128) {
+                        t.direct_tile[c] = v;
+                        found |= 1 << (kClasses + 1 + c);
+                    }
+                }
             }
             const std::string k = cache_key("walk_group", -1);
             if (line.compare(0, k.size(), k) == 0) {
@@ -586,7 +611,9 @@ private:
                 }
             }
         }
-        if (found != (1 << (kClasses + 1)) - 1) return false;
+        if (found != (1 << (2 * kClasses + 1)) - 1) return false;
+        for (int c = 0; c < kClasses; ++c)
+            if (!valid_shape(t.direct_ipt[c], t.direct_tile[c])) return false;
         t.tuned = 1;
         tuning_ = t;
         return true;
@@ -605,7 +632,10 @@ private:
         std::ofstream f(path, std::ios::trunc);
         if (!f) return;  // the cache is an optimisation: an unwritable path is not an error
         for (const auto& l : keep) f << l << "\n";
-        for (int c = 0; c < kClasses; ++c) f << cache_key("direct_ipt", c) << tuning_.direct_ipt[c] << "\n";
+        for (int c = 0; c < kClasses; ++c) {
+            f << cache_key("direct_ipt", c) << tuning_.direct_ipt[c] << "\n";
+            f << cache_key("direct_tile", c) << tuning_.direct_tile[c] << "\n";
+        }
         f << cache_key("walk_group", -1) << tuning_.walk_group << "\n";
     }
 

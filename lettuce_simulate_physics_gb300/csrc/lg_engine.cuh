@@ -34,7 +34,7 @@ struct BodyArrays {
 // Direct-sum launch shape, chosen by the host (autotuned or defaults).
 struct DirectShape {
     int ipt = 4;        // i-bodies per thread: 1, 2, 4 or 8
-    int tile = 256;     // j-bodies per shared-memory stage (multiple of the block size)
+    int tile = 256;     // j-bodies per shared-memory stage: 256, or 128 (ipt 1, 2 or 4)
     int slices = 1;     // j-range splits (split-j); partial sums reduced in a second kernel
 };
 
@@ -77,7 +77,8 @@ struct alignas(32) DirectWork {
     int sys, pad0, pad1;
 };
 int direct_block_bodies(int ipt);
-void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, float G, bool potential,
-                         bool eps0, float4* acc, unsigned* err, cudaStream_t s);
+// tile: j-bodies per shared-memory stage, 256 or 128 (with 1, 2 or 4 i-bodies per thread).
+void launch_direct_batch(const BodyArrays b, const DirectWork* work, int nwork, int ipt, int tile, float G,
+                         bool potential, bool eps0, float4* acc, unsigned* err, cudaStream_t s);
 
 }  // namespace lg

@@ -38,6 +38,7 @@ class EnsembleTuning:
     direct_ipt: tuple
     walk_group: int
     tuned: bool
+    direct_tile: tuple = (256, 256, 256)
 
 
 class Ensemble:
@@ -118,12 +119,14 @@ class Ensemble:
     def tuning(self) -> EnsembleTuning:
         t = _CEnsTuning()
         _check(self._lib.lg_ensemble_get_tuning(self._h, C.byref(t)))
-        return EnsembleTuning(tuple(int(v) for v in t.direct_ipt), int(t.walk_group), bool(t.tuned))
+        return EnsembleTuning(tuple(int(v) for v in t.direct_ipt), int(t.walk_group), bool(t.tuned),
+                              tuple(int(v) for v in t.direct_tile))
 
-    def set_tuning(self, direct_ipt, walk_group: int) -> None:
+    def set_tuning(self, direct_ipt, walk_group: int, direct_tile=(256, 256, 256)) -> None:
         t = _CEnsTuning()
         for k in range(3):
             t.direct_ipt[k] = int(direct_ipt[k])
+            t.direct_tile[k] = int(direct_tile[k])
         t.walk_group = int(walk_group)
         t.tuned = 1
         _check(self._lib.lg_ensemble_set_tuning(self._h, C.byref(t)))

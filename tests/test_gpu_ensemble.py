@@ -6,7 +6,7 @@ recovery path for sync-free tree builds; per-system energies; the autotuner and 
 Bit-exactness holds because each system's tree in the forest equals its single-system tree
 (same frame, keys, topology and moments), the walk visits the same lists, and the batched direct
 kernel does each system's sums with the same tiles as the plain kernel without split-j (set with
-LETTUCE_GB300_DIRECT="ipt,1" for the plain engine). Accuracy against the FP64 direct sum:
+LETTUCE_GB300_DIRECT="ipt,1,tile" for the plain engine). Accuracy against the FP64 direct sum:
 relative rms <= 1e-5 for direct systems and <= 3e-3 for tree systems at theta 0.5."""
 import os
 
@@ -72,11 +72,12 @@ def ensemble_from(workload):
 
 def plain_engine(k, workload, tuning):
     """A plain engine for system k; direct systems without split-j and with the ensemble's i-bodies
-    per thread, so the sums are formed in the same order."""
+    per thread and j-tile, so the sums are formed in the same order."""
     b, counts, eps, theta, methods = workload
     n = int(counts[k])
     cls = 0 if n < 2048 else (1 if n < 4096 else 2)
-    with env(LETTUCE_GB300_DIRECT=f"{tuning.direct_ipt[cls]},1", LETTUCE_CUDA_GROUP=str(tuning.walk_group)):
+    with env(LETTUCE_GB300_DIRECT=f"{tuning.direct_ipt[cls]},1,{tuning.direct_tile[cls]}",
+             LETTUCE_CUDA_GROUP=str(tuning.walk_group)):
         return L.CudaBackend(0)
 
 
@@ -280,6 +281,7 @@ def test_autotuner_and_cache(workload, tmp_path):
         en = ensemble_from(workload)
         t = en.tune()
         assert t.tuned and all(v in (1, 2, 4) for v in t.direct_ipt) and t.walk_group in (64, 96, 128)
+        assert all(v in (128, 256) for v in t.direct_tile)
         assert os.path.exists(cache)
         en2 = ensemble_from(workload)
         t2 = en2.tune()  # loaded from the cache
@@ -288,8 +290,35 @@ def test_autotuner_and_cache(workload, tmp_path):
         en2.run(DT, 2, use_graph=True)
         e, _, _ = en2.energy()
         assert np.all(np.isfinite(e))
-    en.set_tuning((2, 2, 2), 96)
+    en.set_tuning((2, 2, 2), 96, (128, 256, 128))
     assert en.tuning().direct_ipt == (2, 2, 2) and en.tuning().walk_group == 96
+    assert en.tuning().direct_tile == (128, 256, 128)
+    with pytest.raises(ValueError):
+        en.set_tuning((8, 2, 2), 96, (128, 256, 256))  # 128-body tiles are built for 1, 2 or 4 i-bodies
+
+
+def test_tile128_forces_bit_exact_vs_plain_engine(workload):
+    """With 128-body j-tiles in every direct class the batched kernel still forms each system's sums
+    as the plain kernel does with the same shape."""
+    b, counts, eps, theta, methods = workload
+    off = offsets(counts)
+    en = ensemble_from(workload)
+    en.set_tuning((1, 2, 4), 128, (128, 128, 128))
+    en.energy()
+    a = en.accel()
+    got = en.download()
+    tun = en.tuning()
+    for k in range(len(counts)):
+        if methods[k] != 0:
+            continue
+        lo, hi = int(off[k]), int(off[k + 1])
+        ga = by_local_id(got.id[lo:hi] - lo, a[:, lo:hi])
+        be = plain_engine(k, workload, tun)
+        be.upload(system_bodies(b, lo, hi))
+        be.compute_forces(plain_params(k, workload), True)
+        ra = by_local_id(be.download().id, be.accel())
+        be.close()
+        assert np.array_equal(ga.view(np.uint32), ra.view(np.uint32)), k
 
 
 def test_upload_rejects_bad_tables(workload):
