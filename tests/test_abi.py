@@ -104,3 +104,48 @@ def test_fp64_sidecar_reader(lib, tmp_path):
         read_fp64_sidecar(path, bad)
     with pytest.raises(RuntimeError):
         read_fp64_sidecar(path, b.subset(np.arange(n - 1)))
+
+
+# ctypes mirrors of the header's structs (backend.py) against the C compiler's layout.
+_MIRRORS = {
+    "lg_force_params": ("_CForceParams", ["G", "eps", "theta", "method"]),
+    "lg_diag": ("_CDiag", ["mass", "ke", "pe", "has_pe", "px", "lz", "cz"]),
+    "lg_phase_times": ("_CTimes", ["force_ms", "walk_ms", "interactions", "comm_ms", "balance_ms"]),
+    "lg_memory_estimate": ("_CMem", ["device", "host"]),
+    "lg_let_tree": ("_CLetTree", ["nodes", "nnodes", "bx", "bm", "nbodies"]),
+    "lg_render_options": ("_CRenderOptions", ["width", "height", "view", "extent", "color"]),
+    "lg_ensemble_stats": ("_CEnsStats", ["run_ms", "steps", "recoveries", "n", "n_direct", "launches_per_step",
+                                         "last_interactions"]),
+    "lg_ensemble_tuning": ("_CEnsTuning", ["direct_ipt", "walk_group", "tuned", "direct_tile"]),
+}
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every struct the Python bindings pass through the C ABI has the header's size and field
+    offsets (a C program built with the system compiler prints them)."""
+    import shutil
+    import subprocess
+    import ctypes as C
+    from lettuce_simulate_physics_gb300 import backend
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lettuce_gb300.h"', "int main(void) {"]
+    for ctype, (_, fields) in _MIRRORS.items():
+        lines.append(f'  printf("{ctype} size %zu\\n", sizeof({ctype}));')
+        for f in fields:
+            lines.append(f'  printf("{ctype} {f} %zu\\n", offsetof({ctype}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        t, f, v = ln.split()
+        got[(t, f)] = int(v)
+    for ctype, (mirror, fields) in _MIRRORS.items():
+        m = getattr(backend, mirror)
+        assert C.sizeof(m) == got[(ctype, "size")], ctype
+        for f in fields:
+            assert getattr(m, f).offset == got[(ctype, f)], (ctype, f)
