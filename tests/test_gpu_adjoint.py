@@ -57,6 +57,7 @@ def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, ever
     assert ex <= 1e-4 and ev <= 1e-4 and em <= 1e-4
     h = 1e-5
     picks = rng.choice(n, size=6, replace=False)
+    worst = 0.0
     for k, i in enumerate(picks):
         c = k % 3
         for arr, grad in ((x0, gx), (v0, gv)):
@@ -69,13 +70,16 @@ def test_adjoint_matches_fp64_adjoint_and_central_differences(be, n, steps, ever
             else:
                 fd = (O.loss_direct_fp64(x0, p, m, G, eps, dt, steps, xstar)
                       - O.loss_direct_fp64(x0, q, m, G, eps, dt, steps, xstar)) / (2 * h)
+            worst = max(worst, abs(grad[i, c] - fd) / abs(fd))
             assert abs(grad[i, c] - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(grad).max(), (i, c, grad[i, c], fd)
         p, q = m.copy(), m.copy()
         p[i] += h * m[i]
         q[i] -= h * m[i]
         fd = (O.loss_direct_fp64(x0, v0, p, G, eps, dt, steps, xstar)
               - O.loss_direct_fp64(x0, v0, q, G, eps, dt, steps, xstar)) / (2 * h * m[i])
+        worst = max(worst, abs(gm[i] - fd) / abs(fd))
         assert abs(gm[i] - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(gm).max(), (i, gm[i], fd)
+    print(f"n={n} steps={steps} {vjp}: worst sampled component vs FP64 central differences {worst:.2e}")
 
 
 @pytest.mark.parametrize("eps", [0.02, 0.0])
