@@ -5,7 +5,10 @@
 // Parity target: the reference CPU backend (src/cpu_backend.cpp:395-664). After an upload (FP64
 // positions equal to the float inputs) the keys, the sort permutation, the node array (lo, hi,
 // first, nchild in the same indices), the cell geometry and the groups are bit-identical to the
-// reference's; the moments use the reference's FP64 operation order without contraction.
+// reference's; the moments use the reference's FP64 operation order, with the fused multiply-adds
+// its compiler forms (GCC's default contraction on x86-64-v3 and aarch64: a product fused into the
+// sum or difference that is its only use) written out as __fma_rn, everything else rounded per
+// operation. rcrit2 and the walk's opening distance use the same fused float forms.
 //
 // Construction (no level-by-level loop, no recursion):
 //  1. bbox and key frame (FP64), keys (src/cpu_backend.cpp:418-428 formula), identity values.
@@ -1094,10 +1097,11 @@ struct Moments {
     float4* q1;     // (qyz, qzz, rcrit2, 0)
 };
 
-// rcrit2 = (2 half / theta + |com - centre|)^2 capped at FLT_MAX (src/cpu_backend.cpp:595-600).
+// rcrit2 = (2 half / theta + |com - centre|)^2 capped at FLT_MAX (src/cpu_backend.cpp:595-600), with
+// |com - centre|^2 as the reference's compiler forms it: fma(dz, dz, fma(dx, dx, dy*dy)).
 __device__ __forceinline__ float rcrit2_of(float cx, float cy, float cz, float4 g, float inv_theta) {
     const float dx = __fsub_rn(cx, g.x), dy = __fsub_rn(cy, g.y), dz = __fsub_rn(cz, g.z);
-    const float s = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const float s = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
     const double r = __dadd_rn(__dmul_rn(static_cast<double>(__fmul_rn(2.f, g.w)), static_cast<double>(inv_theta)),
                                __dsqrt_rn(static_cast<double>(s)));
     const double r2 = __dmul_rn(r, r);
@@ -1118,6 +1122,7 @@ __device__ void store_moments(Moments mo, uint32_t node, double M, double cx, do
 #define DADD __dadd_rn
 #define DMUL __dmul_rn
 #define DSUB __dsub_rn
+#define DFMA __fma_rn
 
 // Upsweep bookkeeping: internal nodes bucketed by depth, leaves bucketed by body count.
 constexpr int NDEP = MAX_DEPTH + 2;  // depth buckets (depth <= MAX_DEPTH + 1 with headroom)
@@ -1210,14 +1215,14 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
     double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
     for (uint32_t i = r.x; i < r.y; ++i) {
         const double m = b.m[i], dx = DSUB(b.x[i], cx), dy = DSUB(b.y[i], cy), dz = DSUB(b.z[i], cz);
-        const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+        const double r2 = DFMA(dz, dz, DFMA(dx, dx, DMUL(dy, dy)));
         const double m3 = DMUL(m, 3.0);
-        qxx = DADD(qxx, DMUL(m, DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
-        qyy = DADD(qyy, DMUL(m, DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
-        qzz = DADD(qzz, DMUL(m, DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
-        qxy = DADD(qxy, DMUL(DMUL(m3, dx), dy));
-        qxz = DADD(qxz, DMUL(DMUL(m3, dx), dz));
-        qyz = DADD(qyz, DMUL(DMUL(m3, dy), dz));
+        qxx = DFMA(m, DFMA(DMUL(3.0, dx), dx, -r2), qxx);
+        qyy = DFMA(m, DFMA(DMUL(3.0, dy), dy, -r2), qyy);
+        qzz = DFMA(m, DFMA(DMUL(3.0, dz), dz, -r2), qzz);
+        qxy = DFMA(DMUL(m3, dx), dy, qxy);
+        qxz = DFMA(DMUL(m3, dx), dz, qxz);
+        qyz = DFMA(DMUL(m3, dy), dz, qyz);
     }
     store_moments(mo, node, M, cx, cy, cz, qxx, qxy, qxz, qyy, qyz, qzz, g, inv_theta);
 }
@@ -1308,14 +1313,14 @@ __global__ void __launch_bounds__(COMBINE_BS) k_combine_level(const uint32_t* __
 #pragma unroll
         for (int sl = 0; sl < 2; ++sl) {
             const double dx = DSUB(ccx[sl], cx), dy = DSUB(ccy[sl], cy), dz = DSUB(ccz[sl], cz);
-            const double r2 = DADD(DADD(DMUL(dx, dx), DMUL(dy, dy)), DMUL(dz, dz));
+            const double r2 = DFMA(dz, dz, DFMA(dx, dx, DMUL(dy, dy)));
             const double m3 = DMUL(m[sl], 3.0);
-            txx[sl] = DADD(static_cast<double>(qa[sl].x), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dx), dx), r2)));
-            tyy[sl] = DADD(static_cast<double>(qa[sl].w), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dy), dy), r2)));
-            tzz[sl] = DADD(static_cast<double>(qb[sl].y), DMUL(m[sl], DSUB(DMUL(DMUL(3.0, dz), dz), r2)));
-            txy[sl] = DADD(static_cast<double>(qa[sl].y), DMUL(DMUL(m3, dx), dy));
-            txz[sl] = DADD(static_cast<double>(qa[sl].z), DMUL(DMUL(m3, dx), dz));
-            tyz[sl] = DADD(static_cast<double>(qb[sl].x), DMUL(DMUL(m3, dy), dz));
+            txx[sl] = DFMA(m[sl], DFMA(DMUL(3.0, dx), dx, -r2), static_cast<double>(qa[sl].x));
+            tyy[sl] = DFMA(m[sl], DFMA(DMUL(3.0, dy), dy, -r2), static_cast<double>(qa[sl].w));
+            tzz[sl] = DFMA(m[sl], DFMA(DMUL(3.0, dz), dz, -r2), static_cast<double>(qb[sl].y));
+            txy[sl] = DFMA(DMUL(m3, dx), dy, static_cast<double>(qa[sl].y));
+            txz[sl] = DFMA(DMUL(m3, dx), dz, static_cast<double>(qa[sl].z));
+            tyz[sl] = DFMA(DMUL(m3, dy), dz, static_cast<double>(qb[sl].x));
         }
         // Quadrupole sums in child order: lane 0 folds qxx and qyy, lane 1 qzz and qxy, lane 2 qxz,
         // lane 3 qyz.

@@ -27,7 +27,8 @@ __device__ __forceinline__ int warp_excl_scan(int v, int lane, int& total) {
 
 // Warp-cooperative depth-first traversal for the group of bodies gr with box (bc, bh), from node
 // `root`. Each step takes up to 32 nodes, one per lane: a node that contains the group, or whose box
-// distance d satisfies d^2 < rcrit2, is opened (src/cpu_backend.cpp:826-828); an accepted leaf of
+// distance d satisfies d^2 < rcrit2, is opened (src/cpu_backend.cpp:826-828; d^2 formed as the
+// reference's compiler forms it, fma(dz, dz, fma(dx, dx, dy*dy))); an accepted leaf of
 // <= SMALL_LEAF bodies is taken as bodies, other accepted nodes as cells; opened leaves give
 // bodies, opened internal nodes push their children. Cells are appended to s.clist and body
 // ranges to s.rlist (ballot-compacted); flush(nc, nr) is called when a list fills and once at the
@@ -116,7 +117,7 @@ __device__ __forceinline__ void traverse(const TreeView& tv, S& s, uint32_t* sta
             const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.x, bc.x)), bh.x), 0.f);
             const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.y, bc.y)), bh.y), 0.f);
             const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.z, bc.z)), bh.z), 0.f);
-            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
             const bool contains = rg.x <= gr.x && gr.y <= rg.y;
             const bool leaf = rg.w == 0;
             if (!contains && d2 >= rc2) {
@@ -225,7 +226,7 @@ __device__ __forceinline__ void traverse_let(const LetView& lv, S& s, uint32_t* 
                 const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.x, bc.x)), bh.x), 0.f);
                 const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.y, bc.y)), bh.y), 0.f);
                 const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(com.z, bc.z)), bh.z), 0.f);
-                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
                 accept = d2 >= rc2;
             }
             if (accept) {

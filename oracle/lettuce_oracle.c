@@ -498,10 +498,20 @@ static void build_node(or_backend* b, uint32_t ni, int level, int depth, double 
     }
 }
 
+/* The reference as its compiler builds it (GCC's default -ffp-contract=fast; FMA on x86-64-v3 and
+ * aarch64) fuses a product into the sum or difference that is its only use: x*x + y*y + z*z becomes
+ * fma(z, z, fma(x, x, y*y)), in float and in double; m*(3*d*d - r2) accumulated into q becomes
+ * fma(m, fma(3*d, d, -r2), q); m*3*d*e into q becomes fma(m*3*d, e, q). This file is built without
+ * contraction, so those fused forms are spelled out where the reference's results depend on them
+ * (opening tests, rcrit2, quadrupoles); products of two floats are exact in double and are left
+ * as they are. */
+static inline float sq3f(float x, float y, float z) { return fmaf(z, z, fmaf(x, x, y * y)); }
+static inline double sq3(double x, double y, double z) { return fma(z, z, fma(x, x, y * y)); }
+
 /* rcrit2 = (2 half / theta + |com - centre|)^2, capped at FLT_MAX (src/cpu_backend.cpp:595-600). */
 static void finish_node(or_node* nd, const or_geo* g, float inv_theta) {
     float dx = nd->cx - g->gx, dy = nd->cy - g->gy, dz = nd->cz - g->gz;
-    double r = (double)(2 * g->half) * inv_theta + sqrt((double)(dx * dx + dy * dy + dz * dz));
+    double r = (double)(2 * g->half) * inv_theta + sqrt((double)sq3f(dx, dy, dz));
     double r2 = r * r;
     nd->rcrit2 = (float)(r2 < (double)FLT_MAX ? r2 : (double)FLT_MAX);
 }
@@ -542,9 +552,10 @@ static void build_octree(or_backend* b, double theta) {
         double qxx = 0, qxy = 0, qxz = 0, qyy = 0, qyz = 0, qzz = 0;
         for (uint32_t i = nd->lo; i < nd->hi; ++i) {
             double mi = b->m[i], dx = b->x[i] - cx, dy = b->y[i] - cy, dz = b->z[i] - cz;
-            double r2 = dx * dx + dy * dy + dz * dz;
-            qxx += mi * (3 * dx * dx - r2); qyy += mi * (3 * dy * dy - r2); qzz += mi * (3 * dz * dz - r2);
-            qxy += mi * 3 * dx * dy; qxz += mi * 3 * dx * dz; qyz += mi * 3 * dy * dz;
+            double r2 = sq3(dx, dy, dz);
+            qxx = fma(mi, fma(3 * dx, dx, -r2), qxx); qyy = fma(mi, fma(3 * dy, dy, -r2), qyy);
+            qzz = fma(mi, fma(3 * dz, dz, -r2), qzz);
+            qxy = fma(mi * 3 * dx, dy, qxy); qxz = fma(mi * 3 * dx, dz, qxz); qyz = fma(mi * 3 * dy, dz, qyz);
         }
         nd->cx = (float)cx; nd->cy = (float)cy; nd->cz = (float)cz; nd->m = (float)M;
         nd->qxx = (float)qxx; nd->qxy = (float)qxy; nd->qxz = (float)qxz;
@@ -567,10 +578,11 @@ static void build_octree(or_backend* b, double theta) {
         for (uint32_t c = nd->first; c < nd->first + nd->nchild; ++c) {
             const or_node* ch = &b->nodes[c];
             double mc = ch->m, dx = ch->cx - cx, dy = ch->cy - cy, dz = ch->cz - cz;
-            double r2 = dx * dx + dy * dy + dz * dz;
-            qxx += ch->qxx + mc * (3 * dx * dx - r2); qyy += ch->qyy + mc * (3 * dy * dy - r2);
-            qzz += ch->qzz + mc * (3 * dz * dz - r2);
-            qxy += ch->qxy + mc * 3 * dx * dy; qxz += ch->qxz + mc * 3 * dx * dz; qyz += ch->qyz + mc * 3 * dy * dz;
+            double r2 = sq3(dx, dy, dz);
+            qxx += fma(mc, fma(3 * dx, dx, -r2), (double)ch->qxx); qyy += fma(mc, fma(3 * dy, dy, -r2), (double)ch->qyy);
+            qzz += fma(mc, fma(3 * dz, dz, -r2), (double)ch->qzz);
+            qxy += fma(mc * 3 * dx, dy, (double)ch->qxy); qxz += fma(mc * 3 * dx, dz, (double)ch->qxz);
+            qyz += fma(mc * 3 * dy, dz, (double)ch->qyz);
         }
         nd->cx = (float)cx; nd->cy = (float)cy; nd->cz = (float)cz; nd->m = (float)M;
         nd->qxx = (float)qxx; nd->qxy = (float)qxy; nd->qxz = (float)qxz;
@@ -631,7 +643,7 @@ static void build_list(const or_backend* b, const or_group* gr, scratch_t* s) {
         float dy = fmaxf(fabsf(nd->cy - gr->by) - gr->hy, 0.f);
         float dz = fmaxf(fabsf(nd->cz - gr->bz) - gr->hz, 0.f);
         int contains = nd->lo <= gr->lo && gr->hi <= nd->hi;
-        if (!contains && dx * dx + dy * dy + dz * dz >= nd->rcrit2) {
+        if (!contains && sq3f(dx, dy, dz) >= nd->rcrit2) {
             if (nd->nchild == 0 && nd->hi - nd->lo <= (uint32_t)SMALL_LEAF) push_bodies(b, s, nd->lo, nd->hi);
             else push_cell(s, nd);
         } else if (nd->nchild == 0) {
@@ -1068,7 +1080,7 @@ or_frozen* or_frozen_create(size_t n, int steps, const uint32_t* nn, const uint3
                 const float dx = fmaxf(fabsf(c[0] - bx) - hx, 0.f);
                 const float dy = fmaxf(fabsf(c[1] - by) - hy, 0.f);
                 const float dz = fmaxf(fabsf(c[2] - bz) - hz, 0.f);
-                const float d2 = (dx * dx + dy * dy) + dz * dz;
+                const float d2 = sq3f(dx, dy, dz);
                 const int contains = r[0] <= glo && ghi <= r[1];
                 const int leaf = r[3] == 0;
                 if (!contains && d2 >= c[3]) {

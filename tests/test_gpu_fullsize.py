@@ -4,8 +4,7 @@
   live reference CPU backend (oracle/_ref, the reference's src/cpu_backend.cpp compiled from its
   sources; the C restatement where that library is absent) on the same uploaded bodies. Morton
   keys, sort permutation, node arrays, cell geometry, all ten moments, groups, leaf count, depth,
-  interaction counts and per-body costs bit for bit (rcrit2 within 2.5e-7 relative, the FP32
-  rounding of the reference's single-precision square); accelerations within 1e-5 relative rms
+  rcrit2, interaction counts and per-body costs bit for bit; accelerations within 1e-5 relative rms
   and per-body median 1e-5 of the reference's (same lists; FP32 summation order and rsqrt differ).
 - Direct, N = 16384 Plummer (seed 1, r < 10a, eps 0.01; the benchmark's plummer16k input): against
   the reference's own direct forces (golden direct_plummer16384, tests/golden/make_golden.py) and
@@ -63,7 +62,7 @@ def test_disk1m_tree_bit_exact_vs_live_reference(be):
         assert np.array_equal(geo[:, k], rg[f]), f
     for k, f in enumerate(("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz")):
         assert np.array_equal(mom[:, k], rn[f]), f
-    np.testing.assert_allclose(mom[:, 10], rn["rcrit2"], rtol=2.5e-7, atol=0)
+    assert np.array_equal(mom[:, 10], rn["rcrit2"]), "rcrit2"
     box, lohi = be.tree_groups()
     cg = cpu.groups()
     assert np.array_equal(lohi[:, 0], cg["lo"]) and np.array_equal(lohi[:, 1], cg["hi"]), "groups"
@@ -83,6 +82,42 @@ def test_disk1m_tree_bit_exact_vs_live_reference(be):
     print(f"disk1m vs {kind}: {len(rn)} nodes, {len(cg)} groups, {ti} interactions; "
           f"acc rel rms {e:.3g}, per-body median {med:.3g}")
     assert e <= 1e-5 and med <= 1e-5
+    cpu.close()
+
+
+def test_collision16m_tree_bit_exact_vs_live_reference(be):
+    """Configuration 4's initial condition, two inclined 8e6-body disks (1.6e7 bodies): keys,
+    permutation, node arrays, groups, interaction counts and per-body costs bit for bit against
+    the reference CPU backend, forces within relative rms 1e-5."""
+    kind = "ref" if O.available("ref") else "port"
+    b, _ = S.collision(8_000_000)
+    b = zero_v(b)
+    n = len(b)
+    p = params(1, 0.005, 0.6)
+    cpu = O.OracleBackend(kind, 0)
+    cpu.upload(b)
+    cpu.compute_forces(O.TREE, 1.0, 0.005, 0.6, False)
+    be.upload(b)
+    be.compute_forces(p, False)
+    assert np.array_equal(be.tree_keys(), cpu.keys()), "Morton keys"
+    assert np.array_equal(be.download().id, cpu.download().id), "sort permutation"
+    rng, mom, _ = be.tree_nodes()
+    rn = cpu.nodes()
+    assert len(rng) == len(rn), "node count"
+    for k, f in enumerate(("lo", "hi", "first", "nchild")):
+        assert np.array_equal(rng[:, k], rn[f]), f
+    for k, f in enumerate(("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz", "rcrit2")):
+        assert np.array_equal(mom[:, k], rn[f]), f
+    box, lohi = be.tree_groups()
+    cg = cpu.groups()
+    assert np.array_equal(lohi[:, 0], cg["lo"]) and np.array_equal(lohi[:, 1], cg["hi"]), "groups"
+    ti = cpu.times()["interactions"]
+    assert be.times().interactions == ti - n
+    ok, cost = be.body_costs()
+    assert ok and np.array_equal(cost, cpu.body_costs() - 1), "per-body costs"
+    e = rel_rms(be.accel()[:3], cpu.accel()[:3])
+    print(f"collision16m vs {kind}: {len(rn)} nodes, {len(cg)} groups, {ti} interactions; acc rel rms {e:.3g}")
+    assert e <= 1e-5
     cpu.close()
 
 

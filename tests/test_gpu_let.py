@@ -71,13 +71,8 @@ def test_export_bit_exact_vs_reference(engines, method):
         assert np.array_equal(getattr(t, c), ref[f"let_{c}"]), c
     rn = ref["let_nodes"].view(LET_NODE_DTYPE).reshape(-1)
     if method == "tree":
-        # Every field bit-exact except rcrit2 (the engine's geometric-cell arithmetic differs from
-        # the reference's by up to 2 ulp, as the tree parity tests state).
-        for f in LET_NODE_DTYPE.names:
-            if f != "rcrit2":
-                assert np.array_equal(t.nodes[f], rn[f]), f
-        ulp = np.abs(t.nodes["rcrit2"].view(np.int32).astype(np.int64) - rn["rcrit2"].view(np.int32))
-        assert ulp.max() <= 2
+        for f in LET_NODE_DTYPE.names:  # every field bit-exact, rcrit2 included
+            assert np.array_equal(t.nodes[f], rn[f]), f
     else:
         for f in ("mass", "rcrit2", "first_child", "child_count", "body_first", "body_count"):
             assert np.array_equal(t.nodes[f], rn[f]), f

@@ -72,7 +72,7 @@ def test_tree_bit_exact_vs_reference_golden(be, name):
             assert np.array_equal(geo[:, k], gg[f]), f
         for k, f in enumerate(("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz")):
             assert np.array_equal(mom[:, k], rn[f]), f
-        np.testing.assert_allclose(mom[:, 10], rn["rcrit2"], rtol=2.5e-7, atol=0)
+        assert np.array_equal(mom[:, 10], rn["rcrit2"]), "rcrit2"
         box, lohi = be.tree_groups()
         rg = ref["groups"]
         assert np.array_equal(lohi[:, 0], rg["lo"]) and np.array_equal(lohi[:, 1], rg["hi"])
@@ -224,7 +224,7 @@ def test_far_escaper_key_restart(be):
 
 def assert_same_tree(be, cpu, n):
     """The engine's tree after a force call is the CPU backend's: keys, permutation, node ranges,
-    cell geometry, moments and walk groups bit for bit, rcrit2 to FP32 rounding, the same depth,
+    cell geometry, moments, rcrit2 and walk groups bit for bit, the same depth,
     leaves, interaction count and per-body costs."""
     assert np.array_equal(be.tree_keys(), cpu.keys()), "Morton keys"
     assert np.array_equal(be.download().id, cpu.download().id), "sort permutation"
@@ -238,7 +238,7 @@ def assert_same_tree(be, cpu, n):
         assert np.array_equal(geo[:, k], rg[f]), f
     for k, f in enumerate(("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz")):
         assert np.array_equal(mom[:, k], rn[f]), f
-    np.testing.assert_allclose(mom[:, 10], rn["rcrit2"], rtol=2.5e-7, atol=0)
+    assert np.array_equal(mom[:, 10], rn["rcrit2"]), "rcrit2"
     box, lohi = be.tree_groups()
     cg = cpu.groups()
     assert np.array_equal(lohi[:, 0], cg["lo"]) and np.array_equal(lohi[:, 1], cg["hi"]), "groups"

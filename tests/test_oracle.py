@@ -45,7 +45,7 @@ def test_port_tree_bit_exact_vs_reference_golden(name):
             assert np.array_equal(nodes[f], ref["nodes"][f]), f
         for f in ("cx", "cy", "cz", "m", "qxx", "qxy", "qxz", "qyy", "qyz", "qzz"):
             assert np.array_equal(nodes[f], ref["nodes"][f]), f
-        np.testing.assert_allclose(nodes["rcrit2"], ref["nodes"]["rcrit2"], rtol=2e-7, atol=0)
+        assert np.array_equal(nodes["rcrit2"], ref["nodes"]["rcrit2"]), "rcrit2"
         assert np.array_equal(be.geo(), ref["geo"])
         assert np.array_equal(be.groups(), ref["groups"])
         assert np.array_equal(be.leaves(), ref["leaves"])
@@ -126,10 +126,11 @@ def test_port_vs_live_reference(n, seed, kind):
     assert np.array_equal(p.keys(), r.keys())
     assert np.array_equal(p.download().id, r.download().id)
     pn, rn = p.nodes(), r.nodes()
-    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qzz"):
+    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qxx", "qxy", "qzz", "rcrit2"):
         assert np.array_equal(pn[f], rn[f]), f
     assert np.array_equal(p.groups(), r.groups())
     assert p.times()["interactions"] == r.times()["interactions"]
+    assert np.array_equal(p.body_costs(), r.body_costs())
     assert rel_rms(p.accel()[:3], r.accel()[:3]) <= 1e-6
 
 
@@ -146,7 +147,7 @@ def test_port_nested_rekeys_vs_live_reference(n, decades):
     assert np.array_equal(p.keys(), r.keys())
     assert np.array_equal(p.download().id, r.download().id)
     pn, rn = p.nodes(), r.nodes()
-    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qzz"):
+    for f in ("first", "nchild", "lo", "hi", "m", "cx", "qxx", "qxy", "qzz", "rcrit2"):
         assert np.array_equal(pn[f], rn[f]), f
     pg, rg = p.geo(), r.geo()
     for f in ("gx", "gy", "gz", "half"):
