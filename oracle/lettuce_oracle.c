@@ -749,7 +749,9 @@ void or_kick(or_backend* b, double dt) {
     const long n = (long)b->n;
 #pragma omp parallel for simd num_threads(b->nt) schedule(static)
     for (long i = 0; i < n; ++i) {
-        b->vx[i] += b->ax[i] * h; b->vy[i] += b->ay[i] * h; b->vz[i] += b->az[i] * h;
+        /* v += a h as the reference's compiler forms it: one fused multiply-add */
+        b->vx[i] = fmaf(b->ax[i], h, b->vx[i]); b->vy[i] = fmaf(b->ay[i], h, b->vy[i]);
+        b->vz[i] = fmaf(b->az[i], h, b->vz[i]);
     }
     b->kick_ms = now_ms() - t0;
     b->t_step = b->kick_ms + b->drift_ms;
@@ -761,7 +763,9 @@ void or_drift(or_backend* b, double dt) {
     const long n = (long)b->n;
 #pragma omp parallel for simd num_threads(b->nt) schedule(static)
     for (long i = 0; i < n; ++i) {
-        b->x[i] += b->vx[i] * h; b->y[i] += b->vy[i] * h; b->z[i] += b->vz[i] * h;
+        /* x += v h, fused as in the reference's build */
+        b->x[i] = fmaf(b->vx[i], h, b->x[i]); b->y[i] = fmaf(b->vy[i], h, b->y[i]);
+        b->z[i] = fmaf(b->vz[i], h, b->z[i]);
     }
     b->has_pot = 0;
     b->tree_ok = 0;

@@ -109,7 +109,8 @@ def test_port_kdk_diagnostics_vs_golden():
     got = np.array([d[k] for k in keys])
     scale = np.abs(ref["diag"]).max()
     np.testing.assert_allclose(got, ref["diag"], rtol=1e-6, atol=1e-9 * scale)
-    # The reference build contracts x += v h into an FMA; states differ in the last bit.
+    # Kick and drift are the reference's fused forms; the accelerations differ in the last bits
+    # (the reference's AVX rsqrt+Newton against the port's 1/sqrt), and so do the states.
     assert abs(be.exact_potential_energy(G, eps) / float(ref["exact_pe"]) - 1) <= 1e-9
     dn = be.download()
     assert np.array_equal(dn.id, ref["id"])
