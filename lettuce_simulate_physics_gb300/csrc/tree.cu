@@ -1233,8 +1233,9 @@ __global__ void k_leaf_moments(const uint32_t* __restrict__ leaf_order, uint32_t
 // per-child FP64 work runs in parallel); each of the reference's sequential child-order sums is
 // then folded by one lane only, from terms shuffled in child order: M, sx, sy, sz by lanes 0..3;
 // qxx and qyy by lane 0, qzz and qxy by lane 1, qxz by lane 2, qyz by lane 3. Lanes 1..3 divide
-// their first sum by M together. Every FP64 operation of the reference is done once, in its order,
-// so the moments are the reference's bit for bit. (On this part an FP64 warp instruction holds a
+// their first sum by M together. Every FP64 operation of the reference, as its compiler forms it
+// (fused multiply-adds included), is done once, in its order, so the moments are the reference's
+// bit for bit. (On this part an FP64 warp instruction holds a
 // scheduler's FP64 unit for about 64 cycles: the form keeps the number of FP64 warp instructions
 // per node low and spreads the nodes of a level over all schedulers.)
 __device__ __forceinline__ double shfl_d(double v, int src_lane) { return __shfl_sync(0xffffffffu, v, src_lane); }
